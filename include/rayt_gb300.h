@@ -1,0 +1,243 @@
+/*
+ * rayt_gb300 - C ABI of the GB300 (sm_103a) per-frame path of rayt: primary-ray
+ * sparse-voxel-octree traversal against a device block cache, miss/hit
+ * feedback, compaction + radix sort + unique of requested block IDs, and
+ * upload of streamed blocks into the cache.
+ *
+ * The reference has no FFI: its boundary is the C++ class API of the OpenCL
+ * renderer.  Each entry point below names the reference member it replaces
+ * (paths relative to the reference project).  Plain pointers and sizes only.
+ *
+ * Conventions
+ *  - Every call returns RAYT_OK (0) or a negative RAYT_E_* status; the message
+ *    of the last failure on the calling thread is rayt_last_error().  Nothing
+ *    exits the process (the reference calls crash() -> exit(),
+ *    rayt/util/common.h:43-53).
+ *  - Handles are opaque and single-threaded (one host thread per handle), as
+ *    the reference's classes are.
+ *  - Device pointers returned by the library are borrowed: valid until the
+ *    owning handle is destroyed (images: until the next frame).
+ *  - A "stream" argument is a cudaStream_t passed as void*; NULL means the
+ *    library's own stream for that handle (or the legacy default stream for
+ *    the stand-alone primitives).
+ */
+#ifndef RAYT_GB300_H_
+#define RAYT_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RAYT_OK 0
+#define RAYT_E_ARG (-1)      /* invalid argument or size */
+#define RAYT_E_IO (-2)       /* file read/write failed */
+#define RAYT_E_FORMAT (-3)   /* block file is malformed */
+#define RAYT_E_OOM (-4)      /* host or device allocation failed */
+#define RAYT_E_CUDA (-5)     /* CUDA runtime error */
+#define RAYT_E_TIMEOUT (-6)  /* a bounded device wait gave up */
+#define RAYT_E_STATE (-7)    /* call not valid in the current state */
+#define RAYT_E_LIMIT (-8)    /* size beyond a documented format/ABI limit */
+
+/* NO_HIT feedback word (rayt/GPU_renderer/kernels/common.cl:14). */
+#define RAYT_NO_HIT 0x7fffffff
+
+const char* rayt_last_error(void);
+/* Library version string. */
+const char* rayt_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* Block file: replaces StoredOctreeLoader (rayt/CPU data/stored-octree-loader.h:14-38). */
+
+typedef struct rayt_tree rayt_tree;
+
+typedef struct {
+  uint32_t nodes_in_block;   /* StoredOctreeHeader::nodes_in_block */
+  uint32_t blocks_count;     /* StoredOctreeHeader::blocks_count */
+  uint32_t root_block_index; /* StoredOctreeHeader::root_block_index */
+  uint32_t block_stride;     /* bytes per block record (header + content) */
+  uint32_t channels_count;   /* including "node links" */
+  uint32_t content_bytes;    /* StoredOctreeLoader::BytesInBlockContent() */
+  uint64_t header_bytes;     /* file offset of block 0 */
+} rayt_tree_info;
+
+typedef struct {
+  uint16_t parent_pointer_index;
+  uint16_t pointed_child_index;
+  uint32_t parent_pointer_value;
+} rayt_block_root;
+
+typedef struct { /* StoredOctreeBlockHeader (rayt/CPU data/stored-octree-block.h:7-23) */
+  uint32_t block_index;
+  uint32_t parent_block_index;
+  uint32_t roots_count;
+  rayt_block_root roots[8];
+} rayt_block_header;
+
+/* StoredOctreeLoader(file) + ReadHeader (stored-octree-loader.cpp:9-19,60-98). */
+int rayt_tree_open(const char* path, rayt_tree** out);
+void rayt_tree_close(rayt_tree* tree);
+/* StoredOctreeLoader::header() (stored-octree-loader.h:19). */
+int rayt_tree_info_get(const rayt_tree* tree, rayt_tree_info* out);
+/* StoredOctreeHeader::channels[i] (stored-octree-channel-set.h:26-27). */
+int rayt_tree_channel(const rayt_tree* tree, int index, int* bytes_in_node, char* name, int name_capacity);
+/* StoredOctreeLoader::LoadBlock (stored-octree-loader.cpp:31-58); content may be NULL. */
+int rayt_tree_load_block(rayt_tree* tree, uint32_t block_index, rayt_block_header* header,
+                         void* content, size_t content_bytes);
+
+/* ------------------------------------------------------------------------ */
+/* Scene building: the reference's BuildOctree (rayt/CPU data/stored-octree-builder.h:40-41)
+ * fed by the sphere known-answer source (rayt/scene sources/stored-octree-test.cpp:317-323)
+ * or the seeded heightfield/sphere benchmark source. */
+
+typedef struct {
+  int depth;          /* grid of 2^depth voxels per axis */
+  uint32_t seed;      /* heightfield seed */
+  int base_cells;     /* value-noise cells across the scene at octave 0 */
+  int octaves;        /* fBm octaves (lacunarity 2, gain 0.5) */
+  int spheres;        /* number of voxelised sphere shells */
+  uint32_t sphere_seed;
+  int min_radius;     /* sphere radius range in voxels (log-uniform) */
+  int max_radius;
+} rayt_terrain_params;
+
+/* WriteTestOctreeSphere (stored-octree-test.cpp:317-323). */
+int rayt_build_sphere_test(const char* path, float cx, float cy, float cz, float radius, int depth,
+                           int nodes_in_block, uint32_t* blocks_out);
+/* BuildOctree over the heightfield(+spheres) source, channels "normals" and "colors". */
+int rayt_build_terrain(const char* path, const rayt_terrain_params* params, int nodes_in_block,
+                       uint32_t* blocks_out, uint64_t* nodes_out);
+
+/* ------------------------------------------------------------------------ */
+/* Device block cache: replaces GPUOctreeCacheManager + GPUOctreeCache + GPUOctreeData
+ * (rayt/GPU data/gpu-octree-cache-manager.h:14-68, gpu-octree-cache.h:10-113,
+ * gpu-octree-data.h:14-52).  Device layout is the reference's cache format
+ * (rayt/doc/cache data format.txt): one buffer per channel of
+ * max_blocks * nodes_in_block nodes, plus max_blocks * 8 far pointers. */
+
+typedef struct rayt_cache rayt_cache;
+
+/* GPUOctreeCacheManager(max_blocks_count, loader, context); max_blocks <= 0 means
+ * every block of the file.  The tree must outlive the cache. */
+int rayt_cache_create(rayt_tree* tree, int max_blocks, rayt_cache** out);
+void rayt_cache_destroy(rayt_cache* cache);
+/* GPUOctreeCacheManager::InitialFillCache (gpu-octree-cache-manager.cpp:60-108). */
+int rayt_cache_initial_fill(rayt_cache* cache);
+/* GPUOctreeCacheManager::root_node_index (gpu-octree-cache-manager.cpp:41-43). */
+int rayt_cache_root_node_index(const rayt_cache* cache, int* out);
+/* GPUOctreeCache::loaded_blocks_count / max_blocks_count. */
+int rayt_cache_blocks(const rayt_cache* cache, int* loaded, int* max_blocks);
+/* GPUOctreeData::ChannelByName(name)->cl_buffer() / far_pointers_buffer()
+ * (gpu-octree-data.cpp:24-31).  name "far pointers" selects the far-pointer buffer. */
+int rayt_cache_device_buffer(rayt_cache* cache, const char* name, void** device_ptr, size_t* bytes);
+/* Copies a cache buffer to host memory (test and tooling helper). */
+int rayt_cache_read_buffer(rayt_cache* cache, const char* name, void* host, size_t bytes);
+/* Session / transaction protocol (gpu-octree-cache-manager.h:24-57). */
+int rayt_cache_start_session(rayt_cache* cache);
+int rayt_cache_start_transaction(rayt_cache* cache);
+int rayt_cache_mark_block_used(rayt_cache* cache, int block_index_in_cache);
+int rayt_cache_mark_parent_used(rayt_cache* cache, int block_index_in_cache);
+int rayt_cache_request_block(rayt_cache* cache, int block_index);
+int rayt_cache_transaction_filled(const rayt_cache* cache, int* out);
+int rayt_cache_session_filled(const rayt_cache* cache, int* out);
+int rayt_cache_end_transaction(rayt_cache* cache);
+int rayt_cache_end_session(rayt_cache* cache);
+
+typedef struct {
+  int64_t uploaded_blocks;   /* blocks streamed into the cache */
+  int64_t pointer_patches;   /* parent link writes (load and unload) */
+  int64_t far_pointer_writes;
+  int64_t bytes_h2d;         /* host->device bytes for block uploads */
+  int64_t bytes_read;        /* bytes read from the block file */
+  double io_seconds;         /* host time spent reading the file */
+} rayt_cache_stats;
+int rayt_cache_stats_get(const rayt_cache* cache, rayt_cache_stats* out);
+
+/* ------------------------------------------------------------------------ */
+/* Renderer: replaces GPURayTracer (rayt/GPU_renderer/gpu-ray-tracer.h:11-55). */
+
+typedef struct rayt_renderer rayt_renderer;
+
+typedef struct { /* Camera (rayt/scene/camera.h:11-76) */
+  float yaw, pitch, roll;      /* degrees */
+  float position[3];
+  float field_of_view;         /* horizontal, degrees */
+  float aspect_ratio;          /* width / height */
+  float near_clip_plane;       /* the reference's default is 0.01 */
+} rayt_camera;
+
+/* Camera::ViewProjectionMatrix().Inverse() (camera.cpp:23-28, mat.cpp:20-107):
+ * the 16 floats (row-major) the reference passes to InitTracingFrame. */
+int rayt_camera_view_proj_inv(const rayt_camera* camera, float out[16]);
+
+/* GPURayTracer(cache_manager, frame_width, frame_height, context). */
+int rayt_renderer_create(rayt_cache* cache, int width, int height, rayt_renderer** out);
+void rayt_renderer_destroy(rayt_renderer* r);
+/* set_frame_time_limit / set_lod_voxel_size (gpu-ray-tracer.h:17-23). */
+int rayt_renderer_set_frame_time_limit(rayt_renderer* r, double seconds);
+int rayt_renderer_set_lod_voxel_size(rayt_renderer* r, float size);
+/* Deterministic frame end: at most max_passes tracing passes (0 = no cap).  The
+ * cap is applied where the reference applies its wall-clock limit. */
+int rayt_renderer_set_max_passes(rayt_renderer* r, int max_passes);
+/* Seeds the hit-window generator; it is the glibc rand() sequence after
+ * srand(seed), which the reference's feedback extractor draws from
+ * (ray-tracing-feedback-extractor.cpp:147). */
+int rayt_renderer_seed(rayt_renderer* r, uint32_t seed);
+/* Keep each pass's dense per-pixel feedback words for rayt_renderer_pass_words. */
+int rayt_renderer_record_passes(rayt_renderer* r, int on);
+/* GPURayTracer::RenderFrame(camera) (gpu-ray-tracer.cpp:66-227), given the
+ * camera's view_proj_inv matrix. */
+int rayt_render_frame(rayt_renderer* r, const float view_proj_inv[16]);
+/* GPURayTracer::out_image(): RGBA8 frame, row 0 at the bottom. */
+int rayt_renderer_image(rayt_renderer* r, void** device_rgba);
+int rayt_renderer_read_image(rayt_renderer* r, void* host_rgba, size_t bytes);
+/* Dense feedback words of pass `pass` of the last frame (recording on). */
+int rayt_renderer_pass_words(rayt_renderer* r, int pass, int32_t* host_words, size_t count);
+
+typedef struct {
+  int passes;                /* tracing passes of the last frame */
+  int faults;                /* fault blocks reported over the frame */
+  int uploaded_blocks;       /* blocks uploaded during the frame */
+  int session_filled;        /* SessionFilledCache() at frame end */
+  int64_t rays_traced;       /* ray casts over the frame (all passes) */
+  float gpu_ms_trace;        /* device time of tracing passes */
+  float gpu_ms_feedback;     /* device time of feedback unique */
+  float gpu_ms_upload;       /* device time of upload kernels and copies */
+  double frame_ms;           /* host wall time of the frame */
+} rayt_frame_stats;
+int rayt_renderer_stats(const rayt_renderer* r, rayt_frame_stats* out);
+
+/* Traces one pass from view_proj_inv against the cache as it is (no feedback,
+ * no uploads) and counts node-link and far-pointer fetches: the algorithmic
+ * byte count of the traversal roofline.  counts = {rays, link fetches, far
+ * fetches, iterations, hits, faults}. */
+int rayt_renderer_count_fetches(rayt_renderer* r, const float view_proj_inv[16], int64_t counts[6]);
+/* Times `reps` back-to-back first passes (ray setup + traversal + shading) on
+ * the renderer's stream with CUDA events; returns milliseconds per pass. */
+int rayt_renderer_time_pass(rayt_renderer* r, const float view_proj_inv[16], int reps, float* ms_per_pass);
+
+/* ------------------------------------------------------------------------ */
+/* Feedback primitives on device arrays of int32. */
+
+/* GPUSort::Sort (rayt/GPU algorithms/gpu-sort.cpp:16-49): ascending signed
+ * sort in place (LSD radix sort, 8-bit digits, decoupled look-back). */
+int rayt_sort_i32(int32_t* device_data, int n, void* stream);
+/* GPUScan::Scan (rayt/GPU algorithms/gpu-scan.cpp:15-43): inclusive prefix
+ * sum in place, wrapping int32 arithmetic. */
+int rayt_scan_i32(int32_t* device_data, int n, void* stream);
+/* RayTracingFeedbackExtractor::GetUnique (ray-tracing-feedback-extractor.cpp:44-98):
+ * NodeToBlock (when nodes_in_block > 0), then the sorted unique values
+ * (signed ascending, RAYT_NO_HIT last when present) into device_unique (n
+ * entries of room); *unique_count (host) receives the count.  Computed as
+ * stream compaction -> LSD radix sort -> unique; the scratch memory is a
+ * device buffer the library keeps per device and grows on demand.
+ * device_words is not modified. */
+int rayt_feedback_unique(const int32_t* device_words, int n, int nodes_in_block,
+                         int32_t* device_unique, int* unique_count, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RAYT_GB300_H_ */

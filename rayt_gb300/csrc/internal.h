@@ -1,0 +1,123 @@
+// Internal declarations shared by the host C++ and the CUDA translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+#include "../../include/rayt_gb300.h"
+
+namespace rayt {
+
+// ---- errors -----------------------------------------------------------------
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+#define RAYT_CUDA_TRY(expr)                                   \
+  do {                                                        \
+    cudaError_t e_ = (expr);                                  \
+    if (e_ != cudaSuccess) return ::rayt::cuda_fail(e_, #expr); \
+  } while (0)
+
+constexpr int32_t kNoHit = 0x7fffffff;
+constexpr uint32_t kRootParent = (1u << 24) - 1;
+
+// ---- traversal ----------------------------------------------------------------
+struct TraceParams {
+  // cache (the reference's cache format)
+  const uint32_t* links;
+  const uint32_t* far_ptrs;
+  const char4* normals;   // may be null
+  const uchar4* colors;   // may be null
+  int root;
+  int nodes_in_block;
+  // frame
+  int width, height;
+  float m[16];            // view_proj_inv, row-major
+  float lod;              // lod_voxel_size
+  float bg[4];            // background colour (0, 216/255, 1, 1)
+  // ray state of faulted rays, indexed by pixel
+  float4* origin;         // xyz origin, w LOD bias
+  float4* dir;            // xyz direction, w LOD coefficient
+  int* fault_parent;
+  // active lists (rays to trace this pass, rays that faulted)
+  const int* active_in;
+  const int* n_active_in;
+  int* active_out;
+  int* n_active_out;
+  // outputs
+  uchar4* image;
+  int* words_dense;       // optional per-pixel feedback words (debug/parity)
+  uint32_t* fault_bits;   // one bit per tree block
+  uint32_t* hit_bits;     // bit 2*cache_block + dup
+  int* n_words;           // number of non-NO_HIT words this pass
+  unsigned long long* counters;  // optional: rays, link fetches, far fetches, iterations, hits, faults
+};
+
+// first: rays come from the camera (every pixel); otherwise from active_in.
+cudaError_t launch_trace(const TraceParams& p, bool first, bool count, int max_active, cudaStream_t s);
+cudaError_t launch_finish(const TraceParams& p, int max_active, cudaStream_t s);
+cudaError_t launch_fill_i32(int* p, int32_t v, size_t n, cudaStream_t s);
+
+// Feedback bitmaps -> the reference's sorted unique array.
+struct UniqueFromBitsParams {
+  const uint32_t* fault_bits;
+  int fault_words;
+  const uint32_t* hit_bits;
+  int hit_words;
+  const int* n_words;
+  int total_pixels;
+  int32_t* unique_out;   // room for fault bits + hit bits + 1
+  int* counts_out;       // [0] unique count (incl. NO_HIT), [1] fault count
+};
+cudaError_t launch_unique_from_bits(const UniqueFromBitsParams& p, cudaStream_t s);
+
+// ---- radix sort / scan / unique -------------------------------------------------
+struct SortScratch {
+  // sizes computed by sort_scratch_bytes
+  size_t bytes;
+};
+size_t feedback_scratch_bytes(int n);
+// Compaction (drop NO_HIT, NodeToBlock), radix sort, unique.  counts_dev[0]
+// receives the unique count (incl. NO_HIT); everything stays on device.
+cudaError_t feedback_unique_device(const int32_t* words, int n, int nib, int32_t* unique_out,
+                                   int* counts_dev, void* scratch, size_t scratch_bytes, cudaStream_t s);
+size_t sort_scratch_bytes(int n);
+cudaError_t sort_i32_device(int32_t* data, int n, void* scratch, size_t scratch_bytes, cudaStream_t s);
+size_t scan_scratch_bytes(int n);
+cudaError_t scan_i32_device(int32_t* data, int n, void* scratch, size_t scratch_bytes, cudaStream_t s);
+// Device error flag set by bounded waits that gave up (decoupled look-back).
+int* device_error_flag();
+
+// ---- block upload --------------------------------------------------------------
+constexpr int kMaxChannels = 8;
+struct UploadParams {
+  const uint8_t* stage;        // block contents, content_bytes apart
+  const int* slots;            // destination cache slot per staged block
+  int blocks;
+  int nodes_in_block;
+  int channels;
+  int chan_bytes[kMaxChannels];
+  uint8_t* chan[kMaxChannels]; // channel 0 = node links
+};
+struct Patch {
+  uint32_t where;  // bit 31: far-pointer buffer, else node-link buffer; low bits: index
+  uint32_t value;
+};
+cudaError_t launch_upload(const UploadParams& p, cudaStream_t s);
+cudaError_t launch_patches(const Patch* patches, int n, uint32_t* links, uint32_t* far_ptrs, cudaStream_t s);
+
+// ---- glibc-compatible rand() stream -------------------------------------------
+// The additive feedback generator behind glibc's rand()/srand() (TYPE_3:
+// r[i] = r[i-3] + r[i-31], 16807 LCG seeding, 310 discarded outputs), as
+// published in descriptions of the glibc random() algorithm.
+class LibcRand {
+ public:
+  explicit LibcRand(uint32_t seed = 1) { Seed(seed); }
+  void Seed(uint32_t seed);
+  int Next();
+ private:
+  int32_t r_[34];
+  int i_ = 0;
+};
+
+}  // namespace rayt
