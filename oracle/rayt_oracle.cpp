@@ -373,7 +373,12 @@ inline uint32_t AsUint(float f) { uint32_t r; std::memcpy(&r, &f, 4); return r; 
 inline float AsFloat(uint32_t u) { float r; std::memcpy(&r, &u, 4); return r; }
 
 // raycast.cl:33-256 (ESVO descent in [1,2]^3 with block-cache faults)
-void Cast(const uint32_t* links, const uint32_t* far, int root, V4 p, V4 d, float coef, float bias, CastResult* r) {
+// Two guards make the reference's undefined reads explicit (both unreachable
+// on a well-formed cache): a pop that lands past the root ends the loop before
+// reading stack[scale >= 23], and a node or far index outside the cache ends
+// the ray with the iteration-limit error.
+void Cast(const uint32_t* links, const uint32_t* far, int root, V4 p, V4 d, float coef, float bias, CastResult* r,
+          uint32_t node_limit, uint32_t far_limit) {
   p.x = p.x + 1; p.y = p.y + 1; p.z = p.z + 1;
   r->fault_block = -1; r->error = 0; r->dup = 0; r->fetches = 0; r->far_fetches = 0;
   uint32_t stack_parent[kSMax + 1];
@@ -405,7 +410,11 @@ void Cast(const uint32_t* links, const uint32_t* far, int root, V4 p, V4 d, floa
       r->error = 1; r->t = t_min; r->node = (int)parent; r->iterations = iter;
       return;
     }
-    if (desc == 0) { desc = links[parent]; ++r->fetches; }
+    if (desc == 0) {
+      if (parent >= node_limit) { r->error = 1; r->t = t_min; r->node = 0; r->iterations = iter; return; }
+      desc = links[parent];
+      ++r->fetches;
+    }
     float tx_corner = px * tx_coef - tx_bias, ty_corner = py * ty_coef - ty_bias, tz_corner = pz * tz_coef - tz_bias;
     float tc_max = std::fmin(std::fmin(tx_corner, ty_corner), tz_corner);
     int shift = idx ^ octant;
@@ -416,9 +425,15 @@ void Cast(const uint32_t* links, const uint32_t* far, int root, V4 p, V4 d, floa
         return;
       }
       uint32_t ofs;
-      if (desc & (1u << 10)) { ofs = far[desc >> 11]; ++r->far_fetches; }
-      else ofs = (desc >> 11) + parent - (1u << 20);
+      if (desc & (1u << 10)) {
+        if ((desc >> 11) >= far_limit) { r->error = 1; r->t = t_min; r->node = (int)parent; r->iterations = iter; return; }
+        ofs = far[desc >> 11];
+        ++r->far_fetches;
+      } else {
+        ofs = (desc >> 11) + parent - (1u << 20);
+      }
       ofs += (uint32_t)__builtin_popcount(desc & (bit - 1) & 255u);
+      if (ofs >= node_limit) { r->error = 1; r->t = t_min; r->node = (int)parent; r->iterations = iter; return; }
       desc = links[ofs];
       ++r->fetches;
       if (!(desc & 255) || tc_max * coef + bias >= scale_exp2) {
@@ -452,6 +467,7 @@ void Cast(const uint32_t* links, const uint32_t* far, int root, V4 p, V4 d, floa
       if (step & 2) diff |= (uint32_t)(AsInt(py) ^ AsInt(py + scale_exp2));
       if (step & 4) diff |= (uint32_t)(AsInt(pz) ^ AsInt(pz + scale_exp2));
       scale = (AsInt((float)diff) >> 23) - 127;
+      if (scale >= kSMax) break;
       scale_exp2 = AsFloat((uint32_t)((scale - kSMax + 127) << 23));
       parent = stack_parent[scale];
       t_max = stack_tmax[scale];
@@ -495,7 +511,8 @@ struct PassCounters { long long rays = 0, fetches = 0, far_fetches = 0, iteratio
 int32_t TracePixel(RayState& s, const Cache& c, const uint32_t* links, const int8_t* normals,
                    const uint8_t* colors, CastResult* res) {
   if (Done(s)) return kNoHit;
-  Cast(links, c.far.data(), c.root_node, s.origin, s.dir, s.dir.w, s.origin.w, res);
+  Cast(links, c.far.data(), c.root_node, s.origin, s.dir, s.dir.w, s.origin.w, res,
+       (uint32_t)c.max_blocks * (uint32_t)c.nib, (uint32_t)c.max_blocks * 8u);
   if (res->error) {
     s.color[0] = 255; s.color[1] = 0; s.color[2] = 0; s.color[3] = 255;
     std::memset(s.mult, 0, 4);

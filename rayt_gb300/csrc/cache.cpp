@@ -1,0 +1,503 @@
+// Device block cache: the reference's GPUOctreeCacheManager + GPUOctreeCache +
+// GPUOctreeData (rayt/GPU data/gpu-octree-cache-manager.cpp:13-212,
+// gpu-octree-cache.cpp:11-313, gpu-octree-data.cpp:8-93).
+//
+// Policy and bookkeeping are the reference's, step for step, because they
+// decide which slot every block lands in and therefore every node index the
+// traversal reports:
+//   * LRU order: least recently used first; MarkBlockAsUsed moves a block and
+//     all its ancestors to the back; session/transaction markers sit in the
+//     same list and count as "hit" once they reach the front
+//     (gpu-octree-cache.cpp:58-76,236-241,295-313).
+//   * UploadBlock: a free slot while there is one, otherwise protect the
+//     parent and evict the LRU block, restoring up to 8 parent links to their
+//     stored values (gpu-octree-cache.cpp:102-293).
+// What differs is the mechanics: the LRU is an intrusive doubly linked list
+// over slot ids with O(1) moves, block/parent lookups are flat arrays, and the
+// device side of a transaction is one pinned host->device copy of all its
+// blocks, one scatter kernel that rewrites links on the device, and one patch
+// kernel - instead of per-channel and per-pointer clEnqueueWriteBuffer calls.
+#include "cache.h"
+
+#include <chrono>
+#include <cstring>
+
+namespace rayt {
+
+namespace {
+inline uint32_t CacheLink(uint32_t mask, bool fault, bool dup, bool far_flag, uint32_t ptr) {
+  return (ptr << 11) | ((far_flag ? 1u : 0u) << 10) | ((dup ? 1u : 0u) << 9) | ((fault ? 1u : 0u) << 8) | mask;
+}
+inline uint32_t NearValue(int64_t from, int64_t to) { return (uint32_t)((1 << 20) + (to - from)); }
+constexpr int kStageBlocksMin = 16;
+constexpr size_t kStageBytes = 32u << 20;  // per half
+}  // namespace
+
+Cache::~Cache() {
+  if (stream_) cudaStreamSynchronize(stream_);
+  for (uint8_t* p : d_chan_) cudaFree(p);
+  cudaFree(d_far_);
+  cudaFree(d_stage_);
+  cudaFree(d_slots_);
+  cudaFree(d_patches_);
+  cudaFreeHost(h_stage_);
+  cudaFreeHost(h_slots_);
+  cudaFreeHost(h_patches_);
+  for (auto& e : stage_free_)
+    if (e) cudaEventDestroy(e);
+  if (stream_) cudaStreamDestroy(stream_);
+}
+
+int Cache::Init(Tree* tree, int max_blocks) {
+  tree_ = tree;
+  nib_ = (int)tree->info.nodes_in_block;
+  max_blocks_ = max_blocks > 0 ? max_blocks : (int)tree->info.blocks_count;
+  const uint64_t nodes = (uint64_t)max_blocks_ * (uint64_t)nib_;
+  // cache-format limits: node indices are int in the feedback words, far
+  // pointer slots (index*8+i) must fit in 21 bits
+  if (nodes >= (1ull << 30)) return fail(RAYT_E_LIMIT, "cache holds >= 2^30 nodes (feedback words overflow)");
+  if ((uint64_t)max_blocks_ * 8 >= (1ull << 21)) return fail(RAYT_E_LIMIT, "cache has >= 2^18 blocks (far pointer index overflows)");
+  if (tree->chan_names.size() > (size_t)kMaxChannels) return fail(RAYT_E_LIMIT, "too many channels");
+  RAYT_CUDA_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  for (size_t c = 0; c < tree->chan_names.size(); ++c) {
+    uint8_t* p = nullptr;
+    const size_t bytes = (size_t)nodes * tree->chan_bytes[c];
+    if (cudaMalloc(&p, bytes) != cudaSuccess) return fail(RAYT_E_OOM, "cache channel allocation failed");
+    d_chan_.push_back(p);
+    chan_bytes_.push_back(tree->chan_bytes[c]);
+    RAYT_CUDA_TRY(cudaMemsetAsync(p, 0, bytes, stream_));
+  }
+  if (cudaMalloc(&d_far_, (size_t)max_blocks_ * 8 * 4) != cudaSuccess) return fail(RAYT_E_OOM, "far pointer allocation failed");
+  RAYT_CUDA_TRY(cudaMemsetAsync(d_far_, 0, (size_t)max_blocks_ * 8 * 4, stream_));
+
+  stride_ = ((size_t)tree->info.content_bytes + 15) & ~(size_t)15;
+  stage_cap_ = (int)std::max<size_t>(kStageBlocksMin, kStageBytes / stride_);
+  if (cudaHostAlloc(&h_stage_, stride_ * stage_cap_ * 2, cudaHostAllocDefault) != cudaSuccess ||
+      cudaMalloc(&d_stage_, stride_ * stage_cap_ * 2) != cudaSuccess ||
+      cudaHostAlloc(&h_slots_, sizeof(int) * stage_cap_ * 2, cudaHostAllocDefault) != cudaSuccess ||
+      cudaMalloc(&d_slots_, sizeof(int) * stage_cap_ * 2) != cudaSuccess)
+    return fail(RAYT_E_OOM, "staging allocation failed");
+  for (auto& e : stage_free_) RAYT_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  patch_cap_ = stage_cap_ * 32 + 64;
+  if (cudaHostAlloc(&h_patches_, sizeof(Patch) * patch_cap_ * 2, cudaHostAllocDefault) != cudaSuccess ||
+      cudaMalloc(&d_patches_, sizeof(Patch) * patch_cap_ * 2) != cudaSuccess)
+    return fail(RAYT_E_OOM, "patch buffer allocation failed");
+
+  slots_.resize((size_t)max_blocks_);
+  block_slot_.assign(tree->info.blocks_count, -1);
+  parent_slot_.assign(tree->info.blocks_count, -1);
+  touched_.assign((size_t)max_blocks_, 0);
+  const int ids = max_blocks_ + kMarkers + 1;
+  prev_.assign(ids, -1);
+  next_.assign(ids, -1);
+  head_ = max_blocks_ + kMarkers;
+  prev_[head_] = next_[head_] = head_;
+  RAYT_CUDA_TRY(cudaStreamSynchronize(stream_));
+  return RAYT_OK;
+}
+
+const void* Cache::channel(const std::string& name, int bytes) const {
+  for (size_t c = 0; c < tree_->chan_names.size(); ++c)
+    if (tree_->chan_names[c] == name && tree_->chan_bytes[c] == bytes) return d_chan_[c];
+  return nullptr;
+}
+
+int Cache::Buffer(const char* name, void** ptr, size_t* bytes) {
+  if (!name) return fail(RAYT_E_ARG, "null buffer name");
+  if (std::string(name) == "far pointers") {
+    if (ptr) *ptr = d_far_;
+    if (bytes) *bytes = (size_t)max_blocks_ * 8 * 4;
+    return RAYT_OK;
+  }
+  for (size_t c = 0; c < tree_->chan_names.size(); ++c)
+    if (tree_->chan_names[c] == name) {
+      if (ptr) *ptr = d_chan_[c];
+      if (bytes) *bytes = (size_t)max_blocks_ * nib_ * chan_bytes_[c];
+      return RAYT_OK;
+    }
+  return fail(RAYT_E_ARG, std::string("no cache channel named ") + name);
+}
+
+// ---- LRU list ----------------------------------------------------------------
+void Cache::Unlink(int id) {
+  next_[prev_[id]] = next_[id];
+  prev_[next_[id]] = prev_[id];
+  prev_[id] = next_[id] = -1;
+}
+void Cache::InsertBefore(int id, int before) {
+  prev_[id] = prev_[before];
+  next_[id] = before;
+  next_[prev_[before]] = id;
+  prev_[before] = id;
+}
+// MarkBlockAsUsed: the block and every ancestor, bottom up, to the MRU end.
+void Cache::Touch(int slot) {
+  for (int s = slot; s != (int)kRootParent; s = slots_[s].parent) {
+    Unlink(s);
+    InsertBefore(s, head_);
+  }
+  DequeueMarkers();
+}
+void Cache::DequeueMarkers() {
+  while (next_[head_] != head_ && next_[head_] >= max_blocks_) {
+    const int id = next_[head_];
+    markers_[id - max_blocks_].hit = true;
+    markers_[id - max_blocks_].live = false;
+    Unlink(id);
+  }
+}
+void Cache::InsertMarker(int k) {
+  DropMarker(k);
+  markers_[k].hit = false;
+  markers_[k].live = true;
+  InsertBefore(max_blocks_ + k, head_);
+}
+void Cache::DropMarker(int k) {
+  if (markers_[k].live) Unlink(max_blocks_ + k);
+  markers_[k].live = false;
+}
+
+// ---- uploads -------------------------------------------------------------------
+void Cache::AddPatch(bool far_buffer, uint32_t index, uint32_t value) {
+  const uint32_t where = far_buffer ? (0x80000000u | index) : index;
+  auto it = patch_at_.find(where);
+  if (it != patch_at_.end()) {
+    patches_[it->second].value = value;  // last write to an address wins
+  } else {
+    patch_at_[where] = (int)patches_.size();
+    patches_.push_back(Patch{where, value});
+  }
+  if (!far_buffer) touched_[index / (uint32_t)nib_] = epoch_;
+  ++stats_.pointer_patches;
+  if (far_buffer) ++stats_.far_pointer_writes;
+}
+
+int Cache::Flush() {
+  if (staged_ == 0 && patches_.empty()) return RAYT_OK;
+  const int h = half_;
+  uint8_t* hs = h_stage_ + stride_ * stage_cap_ * h;
+  uint8_t* ds = d_stage_ + stride_ * stage_cap_ * h;
+  if (staged_ > 0) {
+    RAYT_CUDA_TRY(cudaMemcpyAsync(ds, hs, stride_ * staged_, cudaMemcpyHostToDevice, stream_));
+    RAYT_CUDA_TRY(cudaMemcpyAsync(d_slots_ + stage_cap_ * h, h_slots_ + stage_cap_ * h, sizeof(int) * staged_,
+                                  cudaMemcpyHostToDevice, stream_));
+    UploadParams up{};
+    up.stage = ds;
+    up.stride = stride_;
+    up.slots = d_slots_ + stage_cap_ * h;
+    up.blocks = staged_;
+    up.nodes_in_block = nib_;
+    up.channels = (int)d_chan_.size();
+    for (int c = 0; c < up.channels; ++c) {
+      up.chan_bytes[c] = chan_bytes_[c];
+      up.chan[c] = d_chan_[c];
+    }
+    RAYT_CUDA_TRY(launch_upload(up, stream_));
+    stats_.bytes_h2d += (int64_t)(stride_ * staged_);
+  }
+  size_t done = 0;
+  while (done < patches_.size()) {
+    const size_t n = std::min(patches_.size() - done, (size_t)patch_cap_);
+    Patch* hp = h_patches_ + (size_t)patch_cap_ * h;
+    Patch* dp = d_patches_ + (size_t)patch_cap_ * h;
+    // the pinned half is reused only after its previous copy finished
+    RAYT_CUDA_TRY(cudaEventSynchronize(stage_free_[h]));
+    std::memcpy(hp, patches_.data() + done, n * sizeof(Patch));
+    RAYT_CUDA_TRY(cudaMemcpyAsync(dp, hp, n * sizeof(Patch), cudaMemcpyHostToDevice, stream_));
+    RAYT_CUDA_TRY(launch_patches(dp, (int)n, reinterpret_cast<uint32_t*>(d_chan_[0]), d_far_, stream_));
+    stats_.bytes_h2d += (int64_t)(n * sizeof(Patch));
+    done += n;
+    if (done < patches_.size()) RAYT_CUDA_TRY(cudaEventRecord(stage_free_[h], stream_));
+  }
+  RAYT_CUDA_TRY(cudaEventRecord(stage_free_[h], stream_));
+  patches_.clear();
+  patch_at_.clear();
+  staged_ = 0;
+  half_ ^= 1;
+  ++epoch_;
+  // the next batch writes into the other half once its last copy is done
+  RAYT_CUDA_TRY(cudaEventSynchronize(stage_free_[half_]));
+  return RAYT_OK;
+}
+
+// UnloadLRUBlock (gpu-octree-cache.cpp:243-293)
+int Cache::Unload() {
+  const int s = next_[head_];
+  if (s == head_ || s >= max_blocks_) {
+    set_error("cache: LRU front is not a block");
+    return -1;
+  }
+  Slot& info = slots_[s];
+  const int p = info.parent;
+  if (p == (int)kRootParent) {
+    set_error("cache: the root block reached the LRU front");
+    return -1;
+  }
+  for (int i = 0; i < info.roots_count; ++i) {
+    uint32_t v = info.ptr_value[i];
+    const uint32_t mask = v & 255u, fault = (v >> 8) & 1u, dup = (v >> 9) & 1u, ptr = v >> 11;
+    if (mask && !fault) v = CacheLink(mask, false, dup != 0, false, NearValue(info.ptr_index[i], ptr));
+    AddPatch(false, (uint32_t)((int64_t)p * nib_ + info.ptr_index[i]), v);
+  }
+  for (int c : info.children) parent_slot_[c] = -1;
+  info.children.clear();
+  Unlink(s);
+  block_slot_[info.block] = -1;
+  DequeueMarkers();
+  return s;
+}
+
+// LoadBlock + UploadBlock (gpu-octree-cache.cpp:102-234); with a queue, fault
+// children are appended for InitialFillCache's breadth-first order.
+int Cache::LoadAndUpload(int block, bool scan_children, std::vector<int>* queue) {
+  const size_t content = tree_->info.content_bytes;
+  if (staged_ == stage_cap_) {
+    int rc = Flush();
+    if (rc != RAYT_OK) return rc;
+  }
+  uint8_t* dst = h_stage_ + stride_ * stage_cap_ * half_ + stride_ * staged_;
+  rayt_block_header hdr;
+  const auto t0 = std::chrono::steady_clock::now();
+  int rc = tree_->LoadBlock((uint32_t)block, &hdr, dst);
+  stats_.io_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (rc != RAYT_OK) return rc;
+  stats_.bytes_read += (int64_t)content + 76;
+  const bool is_root = hdr.parent_block_index == kRootParent;
+  const int root_child = hdr.roots[0].pointed_child_index;
+  if (!is_root && parent_slot_[block] < 0) return fail(RAYT_E_STATE, "cache: parent of a requested block is not resident");
+
+  int s;
+  if (first_free_ == max_blocks_) {
+    if (!is_root) Touch(parent_slot_[block]);  // MarkParentAsUsed(block, global)
+    s = Unload();
+    if (s < 0) return RAYT_E_STATE;
+  } else {
+    s = first_free_++;
+  }
+  if (touched_[s] == epoch_) {
+    // The slot was written or patched earlier in this batch: a batch applies
+    // all block contents before all patches, so submit what is staged (with
+    // the eviction's restore patches) first, then stage this block anew.
+    std::vector<uint8_t> keep(dst, dst + content);
+    rc = Flush();
+    if (rc != RAYT_OK) return rc;
+    dst = h_stage_ + stride_ * stage_cap_ * half_ + stride_ * staged_;
+    std::memcpy(dst, keep.data(), content);
+  }
+  h_slots_[stage_cap_ * half_ + staged_] = s;
+  ++staged_;
+  touched_[s] = epoch_;
+
+  Slot& info = slots_[s];
+  const uint32_t* links = reinterpret_cast<const uint32_t*>(dst);
+  for (int n = 0; n < nib_; ++n) {
+    const uint32_t l = links[n], mask = l & 255u, fault = (l >> 8) & 1u, ptr = l >> 11;
+    if (!mask) continue;
+    if (!fault) {
+      // children inside the block: every one of them must be a node of the block
+      if (ptr + (uint32_t)__builtin_popcount(mask) > (uint32_t)nib_)
+        return fail(RAYT_E_FORMAT, "child link points past the end of its block");
+      continue;
+    }
+    if (ptr >= tree_->info.blocks_count) return fail(RAYT_E_FORMAT, "fault link points past the last block");
+    if (parent_slot_[ptr] < 0) {
+      parent_slot_[ptr] = s;
+      info.children.push_back((int)ptr);
+    }
+    if (scan_children && queue) queue->push_back((int)ptr);
+  }
+  ++stats_.uploaded_blocks;
+
+  if (!is_root) {
+    const int ps = parent_slot_[block];
+    info.parent = ps;
+    info.roots_count = (int)hdr.roots_count;
+    for (uint32_t i = 0; i < hdr.roots_count; ++i) {
+      const rayt_block_root& r = hdr.roots[i];
+      const uint32_t pv = r.parent_pointer_value;
+      if (r.parent_pointer_index >= nib_ || r.pointed_child_index >= nib_ ||
+          (((pv >> 8) & 1u) && (pv & 255u) && (pv >> 11) >= tree_->info.blocks_count))
+        return fail(RAYT_E_FORMAT, "block root record is out of range");
+      info.ptr_index[i] = r.parent_pointer_index;
+      info.ptr_value[i] = r.parent_pointer_value;
+      const int64_t absolute = (int64_t)s * nib_ + r.pointed_child_index;
+      const int64_t ptr_at = (int64_t)ps * nib_ + r.parent_pointer_index;
+      const bool far_flag = (ptr_at > absolute ? ptr_at - absolute : absolute - ptr_at) >= (1 << 20);
+      uint32_t ptr;
+      if (far_flag) {
+        ptr = (uint32_t)s * 8 + i;
+        AddPatch(true, ptr, (uint32_t)absolute);
+      } else {
+        ptr = NearValue(ptr_at, absolute);
+      }
+      // a root whose stored parent pointer is not a fault duplicates a node of
+      // the parent block (gpu-octree-cache.cpp:207-208)
+      AddPatch(false, (uint32_t)ptr_at, CacheLink(pv & 255u, false, ((pv >> 8) & 1u) == 0, far_flag, ptr));
+    }
+  } else {
+    info.parent = (int)kRootParent;
+    info.roots_count = 0;
+  }
+  block_slot_[block] = s;
+  info.block = block;
+  InsertBefore(s, next_[head_]);  // LRU front, then MarkBlockAsUsed
+  Touch(s);
+  if (is_root) root_node_ = s * nib_ + root_child;
+  return RAYT_OK;
+}
+
+// InitialFillCache (gpu-octree-cache-manager.cpp:60-108)
+int Cache::InitialFill() {
+  std::vector<int> queue{(int)tree_->info.root_block_index};
+  size_t head = 0;
+  while (first_free_ < max_blocks_ && head < queue.size()) {
+    const int index = queue[head++];
+    if (block_slot_[index] >= 0) continue;
+    int rc = LoadAndUpload(index, true, &queue);
+    if (rc != RAYT_OK) return rc;
+  }
+  int rc = Flush();
+  if (rc != RAYT_OK) return rc;
+  RAYT_CUDA_TRY(cudaStreamSynchronize(stream_));
+  return RAYT_OK;
+}
+
+int Cache::StartSession() {
+  if (in_session_) return fail(RAYT_E_STATE, "session already started");
+  in_session_ = true;
+  InsertMarker(kSession);
+  return RAYT_OK;
+}
+int Cache::StartTransaction() {
+  if (in_transaction_ || !in_session_) return fail(RAYT_E_STATE, "transaction needs an open session");
+  in_transaction_ = true;
+  InsertMarker(kTransaction);
+  return RAYT_OK;
+}
+int Cache::MarkBlockUsed(int slot) {
+  if (slot < 0 || slot >= first_free_) return fail(RAYT_E_ARG, "cache slot out of range");
+  Touch(slot);
+  return RAYT_OK;
+}
+int Cache::MarkParentUsed(int slot) {
+  if (slot < 0 || slot >= first_free_) return fail(RAYT_E_ARG, "cache slot out of range");
+  const int p = slots_[slot].parent;
+  if (p == (int)kRootParent) DequeueMarkers();
+  else Touch(p);
+  return RAYT_OK;
+}
+// RequestBlock (gpu-octree-cache-manager.cpp:138-148)
+int Cache::RequestBlock(int block) {
+  if (!in_transaction_) return fail(RAYT_E_STATE, "request outside a transaction");
+  if (block < 0 || block >= (int)tree_->info.blocks_count) return fail(RAYT_E_ARG, "block index out of range");
+  if (block_slot_[block] >= 0) return RAYT_OK;
+  if (parent_slot_[block] < 0) return fail(RAYT_E_STATE, "requested block has no resident parent");
+  pending_.push_back(block);
+  Touch(parent_slot_[block]);
+  return RAYT_OK;
+}
+// EndRequestTransaction (gpu-octree-cache-manager.cpp:150-194)
+int Cache::EndTransaction() {
+  if (!in_transaction_) return fail(RAYT_E_STATE, "no open transaction");
+  int rc = RAYT_OK;
+  for (size_t i = 0; i < pending_.size(); ++i) {
+    if (TransactionFilled()) break;
+    rc = LoadAndUpload(pending_[i], false, nullptr);
+    if (rc != RAYT_OK) break;
+  }
+  pending_.clear();
+  const int frc = Flush();
+  in_transaction_ = false;
+  DropMarker(kTransaction);
+  return rc != RAYT_OK ? rc : frc;
+}
+int Cache::EndSession() {
+  if (!in_session_ || in_transaction_) return fail(RAYT_E_STATE, "no open session (or a transaction is open)");
+  in_session_ = false;
+  DropMarker(kSession);
+  return RAYT_OK;
+}
+
+}  // namespace rayt
+
+// ---- C ABI -----------------------------------------------------------------------
+using rayt::fail;
+namespace {
+rayt::Cache* C(rayt_cache* c) { return reinterpret_cast<rayt::Cache*>(c); }
+const rayt::Cache* C(const rayt_cache* c) { return reinterpret_cast<const rayt::Cache*>(c); }
+}  // namespace
+
+extern "C" {
+
+int rayt_cache_create(rayt_tree* tree, int max_blocks, rayt_cache** out) {
+  if (!tree || !out) return fail(RAYT_E_ARG, "rayt_cache_create: null argument");
+  rayt::Cache* c = new rayt::Cache();
+  int rc = c->Init(reinterpret_cast<rayt::Tree*>(tree), max_blocks);
+  if (rc != RAYT_OK) {
+    delete c;
+    return rc;
+  }
+  *out = reinterpret_cast<rayt_cache*>(c);
+  return RAYT_OK;
+}
+void rayt_cache_destroy(rayt_cache* c) { delete C(c); }
+int rayt_cache_initial_fill(rayt_cache* c) { return c ? C(c)->InitialFill() : fail(RAYT_E_ARG, "null cache"); }
+int rayt_cache_root_node_index(const rayt_cache* c, int* out) {
+  if (!c || !out) return fail(RAYT_E_ARG, "null argument");
+  *out = C(c)->root_node();
+  return RAYT_OK;
+}
+int rayt_cache_blocks(const rayt_cache* c, int* loaded, int* max_blocks) {
+  if (!c) return fail(RAYT_E_ARG, "null cache");
+  if (loaded) *loaded = C(c)->loaded();
+  if (max_blocks) *max_blocks = C(c)->max_blocks();
+  return RAYT_OK;
+}
+int rayt_cache_device_buffer(rayt_cache* c, const char* name, void** ptr, size_t* bytes) {
+  return c ? C(c)->Buffer(name, ptr, bytes) : fail(RAYT_E_ARG, "null cache");
+}
+int rayt_cache_read_buffer(rayt_cache* c, const char* name, void* host, size_t bytes) {
+  if (!c || !host) return fail(RAYT_E_ARG, "null argument");
+  void* d = nullptr;
+  size_t have = 0;
+  int rc = C(c)->Buffer(name, &d, &have);
+  if (rc != RAYT_OK) return rc;
+  if (bytes > have) return fail(RAYT_E_ARG, "read larger than the buffer");
+  RAYT_CUDA_TRY(cudaStreamSynchronize(C(c)->stream()));
+  RAYT_CUDA_TRY(cudaMemcpy(host, d, bytes, cudaMemcpyDeviceToHost));
+  return RAYT_OK;
+}
+int rayt_cache_start_session(rayt_cache* c) { return c ? C(c)->StartSession() : fail(RAYT_E_ARG, "null cache"); }
+int rayt_cache_start_transaction(rayt_cache* c) { return c ? C(c)->StartTransaction() : fail(RAYT_E_ARG, "null cache"); }
+int rayt_cache_mark_block_used(rayt_cache* c, int slot) {
+  if (!c) return fail(RAYT_E_ARG, "null cache");
+  if (!C(c)->in_transaction()) return fail(RAYT_E_STATE, "mark outside a transaction");
+  return C(c)->MarkBlockUsed(slot);
+}
+int rayt_cache_mark_parent_used(rayt_cache* c, int slot) {
+  if (!c) return fail(RAYT_E_ARG, "null cache");
+  if (!C(c)->in_transaction()) return fail(RAYT_E_STATE, "mark outside a transaction");
+  return C(c)->MarkParentUsed(slot);
+}
+int rayt_cache_request_block(rayt_cache* c, int block) { return c ? C(c)->RequestBlock(block) : fail(RAYT_E_ARG, "null cache"); }
+int rayt_cache_transaction_filled(const rayt_cache* c, int* out) {
+  if (!c || !out) return fail(RAYT_E_ARG, "null argument");
+  if (!C(c)->in_transaction()) return fail(RAYT_E_STATE, "no open transaction");
+  *out = C(c)->TransactionFilled() ? 1 : 0;
+  return RAYT_OK;
+}
+int rayt_cache_session_filled(const rayt_cache* c, int* out) {
+  if (!c || !out) return fail(RAYT_E_ARG, "null argument");
+  if (!C(c)->in_session()) return fail(RAYT_E_STATE, "no open session");
+  *out = C(c)->SessionFilled() ? 1 : 0;
+  return RAYT_OK;
+}
+int rayt_cache_end_transaction(rayt_cache* c) { return c ? C(c)->EndTransaction() : fail(RAYT_E_ARG, "null cache"); }
+int rayt_cache_end_session(rayt_cache* c) { return c ? C(c)->EndSession() : fail(RAYT_E_ARG, "null cache"); }
+int rayt_cache_stats_get(const rayt_cache* c, rayt_cache_stats* out) {
+  if (!c || !out) return fail(RAYT_E_ARG, "null argument");
+  *out = C(c)->stats();
+  return RAYT_OK;
+}
+
+}  // extern "C"

@@ -30,6 +30,8 @@ struct TraceParams {
   const uchar4* colors;   // may be null
   int root;
   int nodes_in_block;
+  uint32_t node_limit;    // nodes in the cache (max_blocks * nodes_in_block)
+  uint32_t far_limit;     // far pointers in the cache (max_blocks * 8)
   // frame
   int width, height;
   float m[16];            // view_proj_inv, row-major
@@ -48,6 +50,7 @@ struct TraceParams {
   uchar4* image;
   int* words_dense;       // optional per-pixel feedback words (debug/parity)
   uint32_t* fault_bits;   // one bit per tree block
+  int fault_bit_limit;    // number of tree blocks (bits in fault_bits)
   uint32_t* hit_bits;     // bit 2*cache_block + dup
   int* n_words;           // number of non-NO_HIT words this pass
   unsigned long long* counters;  // optional: rays, link fetches, far fetches, iterations, hits, faults
@@ -91,7 +94,8 @@ int* device_error_flag();
 // ---- block upload --------------------------------------------------------------
 constexpr int kMaxChannels = 8;
 struct UploadParams {
-  const uint8_t* stage;        // block contents, content_bytes apart
+  const uint8_t* stage;        // block contents, `stride` bytes apart
+  size_t stride;               // content bytes rounded up to 16 (keeps every block aligned)
   const int* slots;            // destination cache slot per staged block
   int blocks;
   int nodes_in_block;

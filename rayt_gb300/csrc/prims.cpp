@@ -1,0 +1,106 @@
+// C ABI of the stand-alone feedback primitives (GPUSort, GPUScan and the
+// feedback extractor's GetUnique).  Scratch memory is a per-device buffer the
+// library grows on demand and keeps; calls on one device are serialised by a
+// mutex, so concurrent host threads do not share it mid-operation.
+#include <mutex>
+#include "internal.h"
+
+namespace rayt {
+namespace {
+struct Scratch {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+std::mutex g_mu;
+Scratch g_scratch[64];
+
+int get_scratch(size_t bytes, void** out) {
+  int dev = 0;
+  RAYT_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(RAYT_E_ARG, "device ordinal out of range");
+  Scratch& s = g_scratch[dev];
+  if (s.bytes < bytes) {
+    if (s.ptr) {
+      RAYT_CUDA_TRY(cudaDeviceSynchronize());
+      cudaFree(s.ptr);
+      s.ptr = nullptr;
+      s.bytes = 0;
+    }
+    if (cudaMalloc(&s.ptr, bytes) != cudaSuccess) return fail(RAYT_E_OOM, "scratch allocation failed");
+    s.bytes = bytes;
+  }
+  *out = s.ptr;
+  return RAYT_OK;
+}
+
+int check_device_error(cudaStream_t s) {
+  RAYT_CUDA_TRY(cudaStreamSynchronize(s));
+  int flag = 0;
+  RAYT_CUDA_TRY(cudaMemcpy(&flag, device_error_flag(), 4, cudaMemcpyDeviceToHost));
+  if (flag) {
+    int zero = 0;
+    cudaMemcpy(device_error_flag(), &zero, 4, cudaMemcpyHostToDevice);
+    return fail(RAYT_E_TIMEOUT, "a bounded device wait gave up (look-back did not complete)");
+  }
+  return RAYT_OK;
+}
+}  // namespace
+}  // namespace rayt
+
+using rayt::fail;
+
+extern "C" {
+
+int rayt_sort_i32(int32_t* data, int n, void* stream) {
+  if (n < 0 || (n > 0 && !data)) return fail(RAYT_E_ARG, "rayt_sort_i32: bad arguments");
+  if (n >= (1 << 30)) return fail(RAYT_E_LIMIT, "rayt_sort_i32: n must be below 2^30");
+  if (n <= 1) return RAYT_OK;
+  std::lock_guard<std::mutex> lock(rayt::g_mu);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  void* scratch = nullptr;
+  const size_t bytes = rayt::sort_scratch_bytes(n);
+  int rc = rayt::get_scratch(bytes, &scratch);
+  if (rc != RAYT_OK) return rc;
+  RAYT_CUDA_TRY(rayt::sort_i32_device(data, n, scratch, bytes, s));
+  return rayt::check_device_error(s);
+}
+
+int rayt_scan_i32(int32_t* data, int n, void* stream) {
+  if (n < 0 || (n > 0 && !data)) return fail(RAYT_E_ARG, "rayt_scan_i32: bad arguments");
+  if (n >= (1 << 30)) return fail(RAYT_E_LIMIT, "rayt_scan_i32: n must be below 2^30");
+  if (n == 0) return RAYT_OK;
+  std::lock_guard<std::mutex> lock(rayt::g_mu);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  void* scratch = nullptr;
+  const size_t bytes = rayt::scan_scratch_bytes(n);
+  int rc = rayt::get_scratch(bytes, &scratch);
+  if (rc != RAYT_OK) return rc;
+  RAYT_CUDA_TRY(rayt::scan_i32_device(data, n, scratch, bytes, s));
+  return rayt::check_device_error(s);
+}
+
+int rayt_feedback_unique(const int32_t* words, int n, int nib, int32_t* unique, int* unique_count, void* stream) {
+  if (n < 0 || !unique_count || (n > 0 && (!words || !unique)) || nib < 0)
+    return fail(RAYT_E_ARG, "rayt_feedback_unique: bad arguments");
+  if (n >= (1 << 30)) return fail(RAYT_E_LIMIT, "rayt_feedback_unique: n must be below 2^30");
+  if (n == 0) {
+    *unique_count = 0;
+    return RAYT_OK;
+  }
+  std::lock_guard<std::mutex> lock(rayt::g_mu);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  void* scratch = nullptr;
+  const size_t bytes = rayt::feedback_scratch_bytes(n) + 256;
+  int rc = rayt::get_scratch(bytes, &scratch);
+  if (rc != RAYT_OK) return rc;
+  int* counts = reinterpret_cast<int*>(static_cast<uint8_t*>(scratch) + (bytes - 256));
+  RAYT_CUDA_TRY(rayt::feedback_unique_device(words, n, nib, unique, counts, scratch, bytes - 256, s));
+  int host = 0;
+  RAYT_CUDA_TRY(cudaMemcpyAsync(&host, counts, 4, cudaMemcpyDeviceToHost, s));
+  rc = rayt::check_device_error(s);
+  if (rc != RAYT_OK) return rc;
+  *unique_count = host;
+  return RAYT_OK;
+}
+
+}  // extern "C"

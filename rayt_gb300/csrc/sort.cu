@@ -233,6 +233,7 @@ __global__ void __launch_bounds__(kThreads) digit_kernel(const uint32_t* in, uin
     const uint32_t k = s_keys[i];
     const uint32_t d = (k >> shift) & 255u;
     const uint32_t pos = s_global[d] + (uint32_t)i - s_tile_start[d];
+    if (pos >= (uint32_t)m) continue;  // only after a look-back gave up (error flag set)
     if (last && final_out) final_out[pos] = (int32_t)(k ^ 0x80000000u);
     else out[pos] = k;
   }
@@ -295,7 +296,7 @@ __global__ void __launch_bounds__(kThreads) unique_kernel(const uint32_t* keys, 
       s_excl = excl;
     }
     if (base + valid == m) {  // last tile: totals and the NO_HIT sentinel
-      int u = (int)(s_excl + run);
+      int u = min((int)(s_excl + run), m);
       if (m < n_total) out[u++] = kNoHit;
       *result = u;
     }
@@ -304,7 +305,7 @@ __global__ void __launch_bounds__(kThreads) unique_kernel(const uint32_t* keys, 
   uint32_t pos = s_excl + s_warp[warp] + incl - cnt;
 #pragma unroll
   for (int r = 0; r < kItems; ++r)
-    if (flags & (1u << r)) out[pos++] = (int32_t)(k[r] ^ 0x80000000u);
+    if ((flags & (1u << r)) && pos < (uint32_t)m) out[pos++] = (int32_t)(k[r] ^ 0x80000000u);
 }
 
 // ---- inclusive scan (wrapping int32) ---------------------------------------------

@@ -130,6 +130,12 @@ __device__ __forceinline__ Cast cast_ray(const TraceParams& p, float4 o, float4 
       break;
     }
     if (desc == 0) {
+      if (parent >= p.node_limit) {  // only reachable from a corrupt cache
+        r.error = 1;
+        r.t = t_min;
+        r.node = 0;
+        break;
+      }
       desc = ld_link(p.links, parent);
       if (kCount) ++*fetches;
     }
@@ -147,12 +153,24 @@ __device__ __forceinline__ Cast cast_ray(const TraceParams& p, float4 o, float4 
       }
       uint32_t ofs;
       if (desc & (1u << 10)) {
+        if ((desc >> 11) >= p.far_limit) {
+          r.error = 1;
+          r.t = t_min;
+          r.node = (int)parent;
+          break;
+        }
         ofs = __ldg(p.far_ptrs + (desc >> 11));
         if (kCount) ++*far_fetches;
       } else {
         ofs = (desc >> 11) + parent - (1u << 20);
       }
       ofs += __popc(desc & (bit - 1) & 255u);
+      if (ofs >= p.node_limit) {
+        r.error = 1;
+        r.t = t_min;
+        r.node = (int)parent;
+        break;
+      }
       desc = ld_link(p.links, ofs);
       if (kCount) ++*fetches;
       if (!(desc & 255u) || tc_max * coef + bias >= scale_exp2) {
@@ -190,6 +208,9 @@ __device__ __forceinline__ Cast cast_ray(const TraceParams& p, float4 o, float4 
       if (step & 4) diff |= (uint32_t)(__float_as_int(pz) ^ __float_as_int(pz + scale_exp2));
       // (float)diff is exact (diff < 2^23), so its exponent is the top bit
       scale = (__float_as_int((float)diff) >> 23) - 127;
+      // popping past the root: the loop ends here (the reference reads one
+      // more stack entry first, whose value it never uses)
+      if (scale >= kSMax) break;
       scale_exp2 = __int_as_float((scale - kSMax + 127) << 23);
       const uint2 e = stack[scale];
       parent = e.x;
@@ -345,7 +366,7 @@ __global__ void __launch_bounds__(kBlockThreads) trace_kernel(const __grid_const
   if (faulted) p.active_out[slot] = pixel;
   // feedback bitmaps (NodeToBlock applied: hits are per cache block)
   const bool is_hit = word != kNoHit && word > 0;
-  warp_set_bit(p.fault_bits, faulted ? c.fault_block : -1);
+  warp_set_bit(p.fault_bits, faulted && c.fault_block < p.fault_bit_limit ? c.fault_block : -1);
   warp_set_bit(p.hit_bits, is_hit ? 2 * (c.node / p.nodes_in_block) + c.dup : -1);
   {
     const unsigned active = __activemask();

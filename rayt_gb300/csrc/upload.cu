@@ -21,9 +21,7 @@ constexpr int kThreads = 256;
 __global__ void __launch_bounds__(kThreads) upload_kernel(const __grid_constant__ UploadParams p) {
   const int b = blockIdx.x;
   const size_t nib = (size_t)p.nodes_in_block;
-  size_t content = 0;
-  for (int c = 0; c < p.channels; ++c) content += nib * (size_t)p.chan_bytes[c];
-  const uint8_t* src = p.stage + (size_t)b * content;
+  const uint8_t* src = p.stage + (size_t)b * p.stride;
   const size_t slot = (size_t)p.slots[b];
 
   // channel 0: node links, stored format -> cache format

@@ -1,0 +1,146 @@
+"""GPU parity: the CUDA path through the C ABI against the golden fixtures made
+by the reference's own code and against the CPU oracle.  Bit-exact throughout:
+node IDs, feedback words, RGBA8 pixels and cache buffers are integers."""
+import os
+
+import numpy as np
+import pytest
+
+import rayt_gb300 as R
+from tests.conftest import libc_srand
+from tests.golden.common import C1_CAMERA, FRAME_CASES, SPHERE_CACHE_CASES, sha
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _scene(path, max_blocks, w, h, lod=1.0, seed=1):
+    ld = R.StoredOctreeLoader(path)
+    cm = R.GPUOctreeCacheManager(max_blocks, ld)
+    cm.InitialFillCache()
+    rt = R.GPURayTracer(cm, w, h)
+    rt.set_lod_voxel_size(lod)
+    rt.set_frame_time_limit(1e30)
+    rt.seed(seed)
+    return ld, cm, rt
+
+
+def _matrix(cam, w, h):
+    c = R.Camera(cam[0], cam[1], cam[2], cam[3:6], cam[6], w / h)
+    return c.view_proj_inv()
+
+
+@pytest.mark.parametrize("name", sorted(SPHERE_CACHE_CASES))
+def test_sphere_cache_contents(trees, golden, name):
+    """InitialFillCache leaves the reference's exact cache buffers
+    (links rewritten to the cache format, far pointers, channels)."""
+    case = SPHERE_CACHE_CASES[name]
+    ld = R.StoredOctreeLoader(trees[case["tree"]])
+    cm = R.GPUOctreeCacheManager(case["max_blocks"], ld)
+    cm.InitialFillCache()
+    g = golden["sphere_cache"][name]
+    assert cm.root_node_index() == g["root"]
+    for cname in ["node links", "node index", "node index % 211", "far pointers"]:
+        assert sha(cm.read_buffer(cname)) == g["hashes"][cname], cname
+
+
+@pytest.mark.parametrize("name", sorted(FRAME_CASES))
+def test_frames_match_reference(trees, golden, name):
+    """Every frame of every golden case: pass count, each pass's feedback
+    words, the image and the cache buffers afterwards."""
+    case = FRAME_CASES[name]
+    w, h = case["size"]
+    ld, cm, rt = _scene(trees[case["tree"]], case["max_blocks"], w, h, case["lod"], case["seed"])
+    rt.record_passes(True)
+    for i, g in enumerate(golden["frames"][name]):
+        rt.RenderFrame(np.array(g["matrix"], np.float32))
+        st = rt.stats()
+        assert st["passes"] == g["passes"], "frame %d" % i
+        for p in range(st["passes"]):
+            assert sha(rt.pass_words(p)) == g["pass_words_sha256"][p], "frame %d pass %d" % (i, p)
+        assert sha(rt.read_image()) == g["image_sha256"], "frame %d" % i
+        assert cm.root_node_index() == g["root"]
+        for cname in ["node links", "normals", "colors", "far pointers"]:
+            assert sha(cm.read_buffer(cname)) == g["cache"][cname], "frame %d %s" % (i, cname)
+
+
+def _oracle_frame(path, max_blocks, w, h, mats, lod=1.0, seed=1):
+    from oracle import oracle as O
+    sc = O.OracleScene(path, max_blocks, w, h, lod)
+    libc_srand(seed)
+    out = [sc.render(m) for m in mats]
+    counters = sc.counters()
+    sc.close()
+    return out, counters
+
+
+@pytest.mark.parametrize("size", [(1920, 1080), (333, 77), (1, 1), (8, 4), (1000, 1)])
+def test_resident_frame_vs_oracle(trees, size):
+    """Odd and full-HD frame sizes on the resident depth-10 scene."""
+    w, h = size
+    m = _matrix(C1_CAMERA, w, h)
+    (ref,), _ = _oracle_frame(trees["terrain10"], 0, w, h, [m])
+    ld, cm, rt = _scene(trees["terrain10"], 0, w, h)
+    rt.RenderFrame(m)
+    np.testing.assert_array_equal(rt.read_image(), ref[1])
+    assert rt.stats()["passes"] == ref[0]
+
+
+EDGE_CAMERAS = {
+    "looking_away": [225.0, 30.0, 0.0, -0.5, 1.5, 1.5, 60.0],       # every ray misses
+    "inside_volume": [10.0, -5.0, 0.0, 0.5, 0.45, 0.5, 90.0],        # origin inside the octree
+    "straight_down": [0.0, -90.0, 0.0, 0.5, 1.2, 0.5, 40.0],         # axis-aligned rays (epsilon clamp)
+    "axis_x": [-90.0, 0.0, 0.0, -0.2, 0.3, 0.5, 30.0],
+    "grazing": [45.0, -1.0, 0.0, -0.1, 0.42, 1.1, 120.0],            # long shallow rays
+    "rolled": [30.0, -20.0, 45.0, 0.1, 0.7, 1.2, 60.0],
+}
+
+
+@pytest.mark.parametrize("name", sorted(EDGE_CAMERAS))
+@pytest.mark.parametrize("lod", [0.0, 1.0, 4.0])
+def test_edge_cameras_vs_oracle(trees, name, lod):
+    w, h = 160, 120
+    m = _matrix(EDGE_CAMERAS[name], w, h)
+    (ref,), _ = _oracle_frame(trees["terrain10"], 0, w, h, [m], lod=lod)
+    ld, cm, rt = _scene(trees["terrain10"], 0, w, h, lod=lod)
+    rt.RenderFrame(m)
+    np.testing.assert_array_equal(rt.read_image(), ref[1])
+
+
+def test_streaming_sequence_vs_oracle(trees):
+    """A longer streamed flythrough at 320x180 (cache 250 of 790 blocks)."""
+    w, h = 320, 180
+    cams = [[a, -25.0 - 0.2 * a, 0.0, 0.5 - 0.6 * np.sin(np.radians(a)), 0.7, 0.5 + 0.6 * np.cos(np.radians(a)), 60.0]
+            for a in range(0, 360, 30)]
+    mats = [_matrix(c, w, h) for c in cams]
+    refs, _ = _oracle_frame(trees["terrain8s"], 250, w, h, mats, seed=99)
+    ld, cm, rt = _scene(trees["terrain8s"], 250, w, h, seed=99)
+    for i, (m, ref) in enumerate(zip(mats, refs)):
+        rt.RenderFrame(m)
+        assert rt.stats()["passes"] == ref[0], i
+        np.testing.assert_array_equal(rt.read_image(), ref[1], err_msg="frame %d" % i)
+
+
+def test_fetch_counts_match_oracle(trees):
+    """The algorithmic byte count of the roofline (node-link and far-pointer
+    fetches per ray) is the same on the GPU as in the oracle."""
+    from oracle import oracle as O
+    w, h = 512, 512
+    m = _matrix(C1_CAMERA, w, h)
+    sc = O.OracleScene(trees["terrain10"], 0, w, h, 1.0)
+    sc.trace_once(m)
+    oc = sc.counters()
+    sc.close()
+    ld, cm, rt = _scene(trees["terrain10"], 0, w, h)
+    gc = rt.count_fetches(m)
+    for k in ["rays", "link_fetches", "far_fetches", "iterations", "hits", "faults"]:
+        assert gc[k] == oc[k], k
+
+
+def test_pass_cap_stops_frame(trees):
+    w, h = 96, 64
+    m = _matrix(C1_CAMERA, w, h)
+    ld, cm, rt = _scene(trees["terrain8s"], 300, w, h)
+    rt.set_max_passes(2)
+    rt.RenderFrame(m)
+    assert rt.stats()["passes"] <= 2

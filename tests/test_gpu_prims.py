@@ -1,0 +1,99 @@
+"""GPU parity of the feedback primitives (sort, scan, unique) against the
+reference's known-answer runs, the oracle and numpy."""
+import os
+
+import numpy as np
+import pytest
+
+import rayt_gb300 as R
+from tests.golden.common import NO_HIT, feedback_words
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def dev(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a, np.int32)).cuda()
+
+
+def host(t):
+    import torch
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def test_sort_scan_known_answers(built):
+    d = np.load(os.path.join(GOLDEN, "sort_scan.npz"))
+    for a, s, c in zip(d["inputs"], d["sorted"], d["scanned"]):
+        x = dev(a)
+        R.GPUSort(x, a.size)
+        np.testing.assert_array_equal(host(x), s)
+        y = dev(a)
+        R.GPUScan(y, a.size)
+        np.testing.assert_array_equal(host(y), c)
+
+
+@pytest.mark.parametrize("n", [1, 2, 31, 4095, 4096, 4097, 65537, (1 << 20) + 3, 1 << 24])
+def test_sort_sizes(built, n):
+    rng = np.random.default_rng(n)
+    a = rng.integers(-2**31, 2**31 - 1, size=n, dtype=np.int64).astype(np.int32)
+    a[: n // 3] = a[0]  # long run of equal keys
+    x = dev(a)
+    R.GPUSort(x, n)
+    np.testing.assert_array_equal(host(x), np.sort(a))
+
+
+def test_sort_extremes(built):
+    a = np.array([2**31 - 1, -2**31, 0, -1, 1, -2**31, 2**31 - 1] * 1000, np.int32)
+    x = dev(a)
+    R.GPUSort(x, a.size)
+    np.testing.assert_array_equal(host(x), np.sort(a))
+
+
+@pytest.mark.parametrize("n", [1, 4096, 4097, 1000003])
+def test_scan_sizes_wrap(built, n):
+    rng = np.random.default_rng(n)
+    a = rng.integers(-2**31, 2**31 - 1, size=n, dtype=np.int64).astype(np.int32)
+    y = dev(a)
+    R.GPUScan(y, n)
+    with np.errstate(over="ignore"):
+        ref = np.cumsum(a.astype(np.int64)).astype(np.uint64).astype(np.uint32).view(np.int32)
+    np.testing.assert_array_equal(host(y), ref)
+
+
+def _unique(words, nib):
+    import torch
+    w = dev(words)
+    out = torch.zeros(max(1, words.size), dtype=torch.int32, device="cuda")
+    cnt = R.feedback_unique(w, words.size, nib, out)
+    res = host(out)[:cnt]
+    np.testing.assert_array_equal(host(w), words)  # input untouched
+    return res
+
+
+def test_feedback_unique_golden(built):
+    d = np.load(os.path.join(GOLDEN, "feedback_unique.npz"))
+    for key in ["small", "c2_like", "all_nohit", "no_nohit"]:
+        np.testing.assert_array_equal(_unique(d[key + "_words"], int(d[key + "_nib"][0])), d[key + "_unique"],
+                                      err_msg=key)
+
+
+@pytest.mark.parametrize("n,nib", [(1, 1), (100, 0), (4096 * 3 + 5, 4096), (1 << 20, 512)])
+def test_feedback_unique_vs_oracle(built, n, nib):
+    from oracle import oracle as O
+    words = feedback_words(n, n + nib)
+    np.testing.assert_array_equal(_unique(words, nib), O.feedback_unique(words, nib))
+
+
+@pytest.mark.parametrize("n", [1 << 24, (1 << 26) + 12345])
+def test_feedback_unique_large_properties(built, n):
+    """At sizes the oracle's merge sort is too slow for: strictly increasing
+    output, NO_HIT last exactly when present, and the same value set as numpy."""
+    words = feedback_words(n, 77)
+    u = _unique(words, 4096)
+    conv = words.astype(np.int64)
+    hit = (conv > 0) & (conv != NO_HIT)
+    conv[hit] = ((((conv[hit] >> 1) - 1) // 4096 + 1) << 1) | (conv[hit] & 1)
+    np.testing.assert_array_equal(u, np.unique(conv).astype(np.int32))
+    assert np.all(np.diff(u.astype(np.int64)) > 0) and u[-1] == NO_HIT

@@ -1,0 +1,109 @@
+"""CPU tests of host logic and the C ABI (no GPU calls)."""
+import ctypes
+import os
+import re
+import struct
+
+import numpy as np
+import pytest
+
+import rayt_gb300 as R
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    text = open(os.path.join(ROOT, "include", "rayt_gb300.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|void|const char\s*\*|size_t)\s+\**(rayt_\w+)\s*\(", text, re.M)))
+
+
+def test_library_exports_every_declared_symbol(built):
+    names = declared_symbols()
+    assert len(names) >= 40
+    L = ctypes.CDLL(R.LIB_PATH)
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_version_and_error_string(built):
+    assert b"sm_103a" in R.lib().rayt_version()
+    with pytest.raises(R.RaytError) as e:
+        R.StoredOctreeLoader("/nonexistent/file.tree")
+    assert e.value.code == -2 and "cannot open" in str(e.value)
+
+
+def _parse_header(path):
+    b = open(path, "rb").read()
+    nib, blocks, root, stride, nch = struct.unpack("<5I", b[:20])
+    pos, ch = 20, []
+    for _ in range(nch):
+        bn, ln = struct.unpack("<2I", b[pos:pos + 8])
+        ch.append((b[pos + 8:pos + 8 + ln].decode(), bn))
+        pos += 8 + ln
+    return nib, blocks, root, stride, ch, pos, b
+
+
+def test_loader_matches_file_layout(trees):
+    for name in ["sphere7", "terrain8s"]:
+        nib, blocks, root, stride, ch, hdr, raw = _parse_header(trees[name])
+        ld = R.StoredOctreeLoader(trees[name])
+        assert (ld.info.nodes_in_block, ld.info.blocks_count, ld.info.root_block_index) == (nib, blocks, root)
+        assert ld.channels == ch and ld.channels[0] == ("node links", 4)
+        assert ld.info.header_bytes == hdr and ld.info.block_stride == stride
+        for bi in [0, blocks // 2, blocks - 1]:
+            h, content = ld.LoadBlock(bi)
+            o = hdr + stride * bi
+            assert h.block_index == bi
+            assert (h.block_index, h.parent_block_index, h.roots_count) == struct.unpack("<3I", raw[o:o + 12])
+            assert bytes(content) == raw[o + 76:o + 76 + ld.info.content_bytes]
+        with pytest.raises(R.RaytError) as e:
+            ld.LoadBlock(blocks)
+        assert e.value.code == -1
+
+
+def test_loader_rejects_corrupt_files(trees, tmp_path):
+    raw = open(trees["sphere3"], "rb").read()
+    bad = tmp_path / "bad.tree"
+    for blob, code in [(raw[:10], -3),                                         # truncated header
+                       (struct.pack("<5I", 0, 1, 0, 100, 1) + raw[20:], -3),   # zero nodes_in_block
+                       (raw[:20] + struct.pack("<2I", 4, 5) + b"links" + raw[38:], -3)]:  # first channel misnamed
+        bad.write_bytes(blob)
+        with pytest.raises(R.RaytError) as e:
+            R.StoredOctreeLoader(str(bad))
+        assert e.value.code == code
+    # a block record cut short reads as an I/O error on LoadBlock
+    bad.write_bytes(raw[:-100])
+    ld = R.StoredOctreeLoader(str(bad))
+    with pytest.raises(R.RaytError) as e:
+        ld.LoadBlock(ld.info.blocks_count - 1)
+    assert e.value.code == -2
+
+
+def test_builder_rejects_bad_arguments(built, tmp_path):
+    with pytest.raises(R.RaytError):
+        R.build_terrain(str(tmp_path / "x.tree"), 0)
+    with pytest.raises(R.RaytError):
+        R.build_terrain(str(tmp_path / "x.tree"), 6, nodes_in_block=4)
+    with pytest.raises(R.RaytError):
+        R.build_terrain("/nonexistent/dir/x.tree", 6)
+
+
+def test_terrain_with_spheres_is_deterministic(built, tmp_path):
+    a, b = tmp_path / "a.tree", tmp_path / "b.tree"
+    na = R.build_terrain(str(a), 7, 1024, spheres=20, min_radius=2, max_radius=16)
+    nb = R.build_terrain(str(b), 7, 1024, spheres=20, min_radius=2, max_radius=16)
+    assert na == nb and a.read_bytes() == b.read_bytes()
+    assert R.build_terrain(str(b), 7, 1024)[1] < na[1]  # spheres add nodes
+
+
+def test_camera_helper_close_to_reference(golden):
+    """The product's camera helper inverts in double precision; the reference
+    inverts in float, so agreement is to float rounding, not bit for bit."""
+    from tests.golden.common import FRAME_CASES
+    for name, case in FRAME_CASES.items():
+        w, h = case["size"]
+        for cam, g in zip(case["cameras"], golden["frames"][name]):
+            c = R.Camera(cam[0], cam[1], cam[2], cam[3:6], cam[6], w / h)
+            m = c.view_proj_inv()
+            ref = np.array(g["matrix"], np.float32)
+            np.testing.assert_allclose(m, ref, rtol=2e-5, atol=2e-6)
