@@ -1,0 +1,484 @@
+"""Benchmark of the per-frame path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload c3|c1|c2]
+
+A step is one frame of the plain per-frame path (RenderFrame: traversal
+passes, feedback unique, cache transaction with block streaming, finish) for
+the frame workloads, and one compaction + radix sort + unique of the feedback
+words for c2.  Workloads (synthetic seeded scenes built by the block-file
+builder; no public dataset is involved):
+  c1  depth-10 fBm heightfield (1024^3), 512x512, whole tree resident
+  c3  depth-12 heightfield + sphere shells (4096^3), 1920x1080 flythrough on
+      a seeded Catmull-Rom spline, block cache capped at 2 GiB, blocks
+      streamed from the file
+  c2  2^28 feedback words: 90% NO_HIT, Zipf(1.1) block IDs over 2^24
+
+--impl reference times the reference algorithm's CPU implementation (the
+oracle restatement in oracle/, all host threads) on the same workload.
+With --gpus N > 1 (torchrun), every rank renders the same workload on its own
+GPU (replicas; the path has no cross-GPU step) and value is the total.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+HBM_FALLBACK_GBS = 6800.0
+SCENE_DIR = os.environ.get("RAYT_SCENE_DIR", "/tmp/rayt_bench_scenes")
+C1_CAMERA = [45.0, -30.0, 0.0, -0.06, 0.66, 1.06, 60.0]
+
+WORKLOADS = {
+    "c1": {"depth": 10, "spheres": 0, "width": 512, "height": 512, "cache_bytes": 0, "lod": 1.0},
+    "c3": {"depth": 12, "spheres": 2000, "width": 1920, "height": 1080, "cache_bytes": 2 << 30, "lod": 1.0},
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=0)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3"])
+    ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU baseline sample")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def dist_setup(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(k)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def hbm_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return HBM_FALLBACK_GBS, "fallback"
+
+
+def profile_traffic(name):
+    """DRAM bytes per launch of the traversal kernel from the committed ncu
+    summary (profiles/<name>.md, line 'traffic_bytes_per_launch: N')."""
+    p = os.path.join(ROOT, "profiles", name + ".md")
+    try:
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+# ---------------------------------------------------------------------------
+def scene_path(wl, local_rank, world):
+    cfg = WORKLOADS[wl]
+    os.makedirs(SCENE_DIR, exist_ok=True)
+    path = os.path.join(SCENE_DIR, "terrain_d%d_s%d_n4096.tree" % (cfg["depth"], cfg["spheres"]))
+    done = path + ".ok"
+    if local_rank == 0 and not os.path.exists(done):
+        import rayt_gb300 as R
+        t = time.time()
+        R.build_terrain(path + ".tmp", cfg["depth"], 4096, spheres=cfg["spheres"], min_radius=8, max_radius=256)
+        os.replace(path + ".tmp", path)
+        open(done, "w").write("%.1f\n" % (time.time() - t))
+    barrier(world)
+    while not os.path.exists(done):
+        time.sleep(0.5)
+    return path
+
+
+def camera_path(wl, frames, w, h):
+    """C1: one fixed camera.  C3: a Catmull-Rom spline through 8 control points
+    drawn with seed 3 inside the scene, looking along the path and 25 deg down."""
+    import rayt_gb300 as R
+    if wl == "c1":
+        c = R.Camera(C1_CAMERA[0], C1_CAMERA[1], C1_CAMERA[2], C1_CAMERA[3:6], C1_CAMERA[6], w / h)
+        m = c.view_proj_inv()
+        return [m] * frames
+    rng = np.random.default_rng(3)
+    pts = np.stack([rng.uniform(0.15, 0.85, 8), rng.uniform(0.62, 0.85, 8), rng.uniform(0.15, 0.85, 8)], 1)
+    pts = np.concatenate([pts, pts[:3]])  # closed loop
+
+    def spline(u):
+        seg = min(int(u), len(pts) - 4)
+        t = u - seg
+        p0, p1, p2, p3 = pts[seg:seg + 4]
+        return 0.5 * ((2 * p1) + (-p0 + p2) * t + (2 * p0 - 5 * p1 + 4 * p2 - p3) * t * t
+                      + (-p0 + 3 * p1 - 3 * p2 + p3) * t * t * t)
+
+    out = []
+    span = len(pts) - 3
+    for i in range(frames):
+        u = span * i / max(1, frames)
+        p = spline(u)
+        q = spline(min(span - 1e-3, u + 0.01))
+        d = q - p
+        yaw = math.degrees(math.atan2(d[0], -d[2]))
+        c = R.Camera(yaw, -25.0, 0.0, tuple(float(v) for v in p), 60.0, w / h)
+        out.append(c.view_proj_inv())
+    return out
+
+
+def cache_blocks(cfg):
+    if not cfg["cache_bytes"]:
+        return 0
+    return int(cfg["cache_bytes"] // (4096 * 12))
+
+
+# ---------------------------------------------------------------------------
+def run_cpu_frames(path, cfg, mats, budget_s):
+    """The oracle (reference algorithm on host cores) over the same frames, until
+    the frames run out or the time budget is spent.  Returns (rays, seconds,
+    frames, setup_seconds)."""
+    from oracle import oracle as O
+    w, h = cfg["width"], cfg["height"]
+    t0 = time.time()
+    sc = O.OracleScene(path, cache_blocks(cfg), w, h, cfg["lod"], 1e30)
+    setup = time.time() - t0
+    rays, el, n = 0, 0.0, 0
+    for m in mats:
+        t = time.time()
+        sc.render(m)
+        el += time.time() - t
+        rays += w * h
+        n += 1
+        if el > budget_s:
+            break
+    sc.close()
+    return rays, el, n, setup
+
+
+def bench_frames(args, rank, world, local):
+    import torch
+
+    import rayt_gb300 as R
+    wl = args.workload
+    cfg = WORKLOADS[wl]
+    w, h = cfg["width"], cfg["height"]
+    steps = args.steps or (300 if wl == "c3" else 200)
+    path = scene_path(wl, local, world)
+    mats = camera_path(wl, args.warmup + steps, w, h)
+    threads = os.cpu_count() or 1
+
+    if args.impl == "reference":
+        if rank != 0:
+            return None
+        rays, el, n, setup = run_cpu_frames(path, cfg, mats[args.warmup:], args.cpu_seconds * 3)
+        v = rays / el / 1e6
+        sample = "%d of %d frames at %dx%d (oracle, OpenMP)" % (n, steps, w, h)
+        return {"metric": "Mrays/s at %dx%d (frames of the per-frame path)" % (w, h), "value": round(v, 3),
+                "unit": "Mrays/s", "impl": "reference", "n_gpus": 1, "steps": n, "warmup": 0,
+                "ms_per_step": round(el / n * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": wl, "width": w, "height": h, "depth": cfg["depth"],
+                           "spheres": cfg["spheres"], "cache_blocks": cache_blocks(cfg)},
+                "cpu_baseline": {"value": round(v, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                                 "sample": sample},
+                "e2e": {"value": round(v, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+    torch.cuda.set_device(local)
+    ld = R.StoredOctreeLoader(path)
+    cm = R.GPUOctreeCacheManager(cache_blocks(cfg), ld)
+    t0 = time.time()
+    cm.InitialFillCache()
+    fill_s = time.time() - t0
+    rt = R.GPURayTracer(cm, w, h)
+    rt.set_lod_voxel_size(cfg["lod"])
+    rt.set_frame_time_limit(1e30)
+    stream = torch.cuda.ExternalStream(rt.stream_handle())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > L2 (129 MB)
+    img = np.zeros((h, w, 4), np.uint8)
+    pinned = torch.empty((h, w, 4), dtype=torch.uint8).pin_memory()
+
+    for i in range(args.warmup):
+        rt.RenderFrame(mats[i])
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms_dev, wall = 0.0, 0.0
+    passes, launches, h2d, d2h, uploaded, trace_ms = 0, 0, 0, 0, 0, 0.0
+    lat = []
+    for i in range(args.warmup, args.warmup + steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(i & 255)  # L2 holds nothing of the previous frame
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t = time.perf_counter()
+        e0.record(stream)
+        rt.RenderFrame(mats[i])
+        e1.record(stream)
+        # end to end: the frame's RGBA8 image read back to pinned host memory
+        R._check(R.lib().rayt_renderer_read_image(rt._h, pinned.data_ptr(), pinned.numel()))
+        wall += time.perf_counter() - t
+        e1.synchronize()
+        d = e0.elapsed_time(e1)
+        ms_dev += d
+        lat.append(d)
+        st = rt.stats()
+        passes += st["passes"]
+        launches += st["kernel_launches"]
+        h2d += st["bytes_h2d"]
+        d2h += st["bytes_d2h"] + w * h * 4
+        uploaded += st["uploaded_blocks"]
+        trace_ms += st["gpu_ms_trace"]
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    t_dev = max_over_ranks(ms_dev / 1e3, world)
+    t_wall = max_over_ranks(wall, world)
+    rays = float(w * h * steps)
+    total_rays = sum_over_ranks(rays, world)
+
+    # roofline of the dominant kernel (first-pass traversal) on the last camera
+    m_last = mats[args.warmup + steps - 1]
+    fetch = rt.count_fetches(m_last)
+    pass_ms = rt.time_pass(m_last, 5)
+    alg_bytes = 4 * fetch["link_fetches"] + 4 * fetch["far_fetches"] + 16 * fetch["rays"]
+    achieved = alg_bytes / (pass_ms / 1e3) / 1e9
+    peak, peak_kind = hbm_peak()
+    traffic = profile_traffic("trace_kernel_%s" % wl)
+
+    cpu = None
+    if rank == 0:
+        crays, cel, cn, _ = run_cpu_frames(path, cfg, mats[args.warmup:], args.cpu_seconds)
+        cpu = {"value": round(crays / cel / 1e6, 3), "unit": "Mrays/s", "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": "%d frames at %dx%d of the same workload (oracle, OpenMP)" % (cn, w, h)}
+    if rank != 0:
+        return None
+    lat_sorted = np.sort(np.array(lat))
+    return {
+        "metric": "Mrays/s at %dx%d (frames of the per-frame path)" % (w, h),
+        "value": round(total_rays / t_dev / 1e6, 3), "unit": "Mrays/s", "n_gpus": world, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": round(t_dev / steps * 1e3, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": wl, "width": w, "height": h, "depth": cfg["depth"], "spheres": cfg["spheres"],
+                   "nodes_in_block": 4096, "cache_blocks": cm.blocks()[1], "tree_blocks": ld.info.blocks_count,
+                   "lod_voxel_size": cfg["lod"], "l2": "flushed between frames (256 MiB write)",
+                   "parallelism": "replicas" if world > 1 else "single GPU", "initial_fill_s": round(fill_s, 2)},
+        "e2e": {"value": round(total_rays / t_wall / 1e6, 3), "unit": "Mrays/s",
+                "h2d_bytes_per_step": int(h2d / steps) + 64, "d2h_bytes_per_step": int(d2h / steps)},
+        "frame_latency_ms": {"p50": round(float(np.percentile(lat_sorted, 50)), 4),
+                             "p99": round(float(np.percentile(lat_sorted, 99)), 4)},
+        "frames": {"passes_per_frame": round(passes / steps, 3), "uploaded_blocks_per_frame": round(uploaded / steps, 2),
+                   "trace_ms_per_frame": round(trace_ms / steps, 4)},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
+                     "kernel": "trace_kernel<first pass>", "launch_ms": round(pass_ms, 4),
+                     "bytes_per_ray": round(alg_bytes / fetch["rays"], 2),
+                     "link_fetches_per_ray": round(fetch["link_fetches"] / fetch["rays"], 3)},
+        "cpu_baseline": cpu,
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+
+
+# ---------------------------------------------------------------------------
+def zipf_words(n, seed=5, blocks=1 << 24, s=1.1):
+    """C2 input: 90% NO_HIT, the rest block IDs ~ Zipf(s) over [0, blocks)
+    (continuous inversion), half as fault words -id-1, half as hit words
+    ((id+1)<<1)|dup."""
+    rng = np.random.default_rng(seed)
+    out = np.full(n, 0x7FFFFFFF, np.int32)
+    m = n // 10
+    idx = rng.choice(n, size=m, replace=False) if n <= (1 << 22) else rng.integers(0, n, size=m)
+    u = rng.random(m)
+    a = 1.0 - s
+    ids = np.floor((1.0 + u * (blocks ** a - 1.0)) ** (1.0 / a)).astype(np.int64) - 1
+    ids = np.clip(ids, 0, blocks - 1)
+    fault = rng.random(m) < 0.5
+    dup = rng.integers(0, 2, size=m)
+    out[idx] = np.where(fault, -ids - 1, ((ids + 1) << 1) | dup).astype(np.int32)
+    return out
+
+
+def bench_c2(args, rank, world, local):
+    import torch
+
+    import rayt_gb300 as R
+    n = 1 << 28
+    steps = args.steps or 20
+    words = zipf_words(n)
+    if args.impl == "reference":
+        if rank != 0:
+            return None
+        from oracle import oracle as O
+        sub = words[: 1 << 22]
+        t = time.time()
+        k = 0
+        while time.time() - t < args.cpu_seconds and k < steps:
+            O.feedback_unique(sub, 4096)
+            k += 1
+        el = (time.time() - t) / k
+        v = sub.size / el / 1e9
+        return {"metric": "Gkeys/s feedback compaction+sort+unique (2^28 words)", "value": round(v, 4),
+                "unit": "Gkeys/s", "impl": "reference", "n_gpus": 1, "steps": k, "warmup": 0,
+                "ms_per_step": round(el * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+                "config": {"workload": "c2", "n": n, "sample_n": sub.size},
+                "cpu_baseline": {"value": round(v, 4), "unit": "Gkeys/s", "cores": os.cpu_count() or 1, "kind": "port",
+                                 "sample": "2^22 of the 2^28 words per step (merge sort + Hillis-Steele scan)"},
+                "e2e": {"value": round(v, 4), "unit": "Gkeys/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    torch.cuda.set_device(local)
+    d_words = torch.from_numpy(words).cuda()
+    d_out = torch.empty(n, dtype=torch.int32, device="cuda")
+    host_words = torch.from_numpy(words).pin_memory()
+    for _ in range(args.warmup):
+        R.feedback_unique(d_words, n, 4096, d_out)
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = ClockSampler(local)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    cnt = 0
+    for _ in range(steps):
+        cnt = R.feedback_unique(d_words, n, 4096, d_out)
+    e1.record()
+    torch.cuda.synchronize()
+    t_dev = max_over_ranks(e0.elapsed_time(e1) / 1e3, world)
+    # end to end: words from pinned host memory, unique array back to host
+    t = time.perf_counter()
+    for _ in range(steps):
+        d_words.copy_(host_words, non_blocking=True)
+        c = R.feedback_unique(d_words, n, 4096, d_out)
+        d_out[:c].cpu()
+    t_e2e = max_over_ranks(time.perf_counter() - t, world)
+    clk = clocks.stop()
+    m = int((words != 0x7FFFFFFF).sum())
+    alg = 4 * n + 4 * m + 32 * m + 4 * m + 4 * cnt
+    achieved = alg / (t_dev / steps) / 1e9
+    peak, kind = hbm_peak()
+    if rank != 0:
+        return None
+    return {"metric": "Gkeys/s feedback compaction+sort+unique (2^28 words)",
+            "value": round(sum_over_ranks(n * steps, world) / t_dev / 1e9, 4), "unit": "Gkeys/s", "n_gpus": world,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": round(t_dev / steps * 1e3, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": "c2", "n": n, "kept": m, "unique": cnt, "l2": "inputs (1 GiB) larger than L2"},
+            "e2e": {"value": round(n * steps / t_e2e / 1e9, 4), "unit": "Gkeys/s", "h2d_bytes_per_step": 4 * n,
+                    "d2h_bytes_per_step": 4 * cnt},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": None, "peak_source": kind},
+            "cpu_baseline": None, "gpu_launches": steps * 7, "clocks": clk}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        # the CPU arm: rank 0 alone runs it; other ranks exit without work
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        rank, world, local = 0, 1, 0
+    else:
+        rank, world, local = dist_setup(args.gpus)
+    if args.workload == "c2":
+        out = bench_c2(args, rank, world, local)
+    else:
+        out = bench_frames(args, rank, world, local)
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

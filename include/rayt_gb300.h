@@ -190,6 +190,9 @@ int rayt_renderer_record_passes(rayt_renderer* r, int on);
 /* GPURayTracer::RenderFrame(camera) (gpu-ray-tracer.cpp:66-227), given the
  * camera's view_proj_inv matrix. */
 int rayt_render_frame(rayt_renderer* r, const float view_proj_inv[16]);
+/* The CUDA stream (cudaStream_t) the renderer and its cache run on, for
+ * callers that order their own work or timing events after a frame. */
+int rayt_renderer_stream(rayt_renderer* r, void** stream);
 /* GPURayTracer::out_image(): RGBA8 frame, row 0 at the bottom. */
 int rayt_renderer_image(rayt_renderer* r, void** device_rgba);
 int rayt_renderer_read_image(rayt_renderer* r, void* host_rgba, size_t bytes);
@@ -206,6 +209,9 @@ typedef struct {
   float gpu_ms_feedback;     /* device time of feedback unique */
   float gpu_ms_upload;       /* device time of upload kernels and copies */
   double frame_ms;           /* host wall time of the frame */
+  int kernel_launches;       /* library kernels launched for the frame */
+  int64_t bytes_h2d;         /* host->device bytes of the frame (block uploads) */
+  int64_t bytes_d2h;         /* device->host bytes of the frame (feedback read-back) */
 } rayt_frame_stats;
 int rayt_renderer_stats(const rayt_renderer* r, rayt_frame_stats* out);
 

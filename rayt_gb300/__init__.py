@@ -63,7 +63,8 @@ class CacheStats(C.Structure):
 class FrameStats(C.Structure):
     _fields_ = [("passes", C.c_int), ("faults", C.c_int), ("uploaded_blocks", C.c_int), ("session_filled", C.c_int),
                 ("rays_traced", C.c_int64), ("gpu_ms_trace", C.c_float), ("gpu_ms_feedback", C.c_float),
-                ("gpu_ms_upload", C.c_float), ("frame_ms", C.c_double)]
+                ("gpu_ms_upload", C.c_float), ("frame_ms", C.c_double), ("kernel_launches", C.c_int),
+                ("bytes_h2d", C.c_int64), ("bytes_d2h", C.c_int64)]
 
 
 class CameraStruct(C.Structure):
@@ -120,6 +121,7 @@ def lib():
         "rayt_renderer_record_passes": (i32, [vp, i32]),
         "rayt_render_frame": (i32, [vp, C.POINTER(f32)]),
         "rayt_renderer_image": (i32, [vp, C.POINTER(vp)]),
+        "rayt_renderer_stream": (i32, [vp, C.POINTER(vp)]),
         "rayt_renderer_read_image": (i32, [vp, vp, C.c_size_t]),
         "rayt_renderer_pass_words": (i32, [vp, i32, vp, C.c_size_t]),
         "rayt_renderer_stats": (i32, [vp, C.POINTER(FrameStats)]),
@@ -334,6 +336,12 @@ class GPURayTracer:
             camera_or_matrix = camera_or_matrix.view_proj_inv()
         m, p = _mat(camera_or_matrix)
         _check(lib().rayt_render_frame(self._h, p))
+
+    def stream_handle(self):
+        """The cudaStream_t (as an int) the renderer runs on."""
+        p = C.c_void_p()
+        _check(lib().rayt_renderer_stream(self._h, C.byref(p)))
+        return p.value or 0
 
     def out_image_device_ptr(self):
         p = C.c_void_p()

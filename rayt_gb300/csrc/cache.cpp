@@ -193,6 +193,7 @@ int Cache::Flush() {
       up.chan[c] = d_chan_[c];
     }
     RAYT_CUDA_TRY(launch_upload(up, stream_));
+    ++launches_;
     stats_.bytes_h2d += (int64_t)(stride_ * staged_);
   }
   size_t done = 0;
@@ -205,6 +206,7 @@ int Cache::Flush() {
     std::memcpy(hp, patches_.data() + done, n * sizeof(Patch));
     RAYT_CUDA_TRY(cudaMemcpyAsync(dp, hp, n * sizeof(Patch), cudaMemcpyHostToDevice, stream_));
     RAYT_CUDA_TRY(launch_patches(dp, (int)n, reinterpret_cast<uint32_t*>(d_chan_[0]), d_far_, stream_));
+    ++launches_;
     stats_.bytes_h2d += (int64_t)(n * sizeof(Patch));
     done += n;
     if (done < patches_.size()) RAYT_CUDA_TRY(cudaEventRecord(stage_free_[h], stream_));

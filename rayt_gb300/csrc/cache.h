@@ -39,6 +39,7 @@ class Cache {
   const void* channel(const std::string& name, int bytes) const;
   int Buffer(const char* name, void** ptr, size_t* bytes);
   const rayt_cache_stats& stats() const { return stats_; }
+  int64_t launches() const { return launches_; }
   int uploaded_since(int64_t mark) const { return (int)(stats_.uploaded_blocks - mark); }
   bool in_transaction() const { return in_transaction_; }
   bool in_session() const { return in_session_; }
@@ -93,6 +94,7 @@ class Cache {
   int epoch_ = 1;
 
   rayt_cache_stats stats_{};
+  int64_t launches_ = 0;   // upload and patch kernels launched
 
   // list helpers
   void Unlink(int id);

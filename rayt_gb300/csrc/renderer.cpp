@@ -37,6 +37,7 @@ class Renderer {
   LibcRand rand;
   rayt_frame_stats stats{};
   uchar4* image() const { return d_image_; }
+  cudaStream_t stream() const { return s_; }
 
  private:
   Cache* cache_ = nullptr;
@@ -208,6 +209,10 @@ int Renderer::Frame(const float* m) {
   stats = rayt_frame_stats{};
   pass_words_.clear();
   const int64_t uploaded0 = cache_->stats().uploaded_blocks;
+  const int64_t launches0 = cache_->launches();
+  const int64_t h2d0 = cache_->stats().bytes_h2d;
+  int launches = 0;
+  int64_t d2h = 0;
   int rc = cache_->StartSession();
   if (rc != RAYT_OK) return rc;
   const int total = w_ * h_;
@@ -224,6 +229,7 @@ int Renderer::Frame(const float* m) {
     p.words_dense = record ? d_dense_ : nullptr;
     RAYT_CUDA_TRY(cudaEventRecord(ev_[0], s_));
     RAYT_CUDA_TRY(launch_trace(p, it == 0, false, active_prev, s_));
+    launches += (it == 0 || active_prev > 0) ? 1 : 0;
     RAYT_CUDA_TRY(cudaEventRecord(ev_[1], s_));
     UniqueFromBitsParams q{};
     q.fault_bits = d_bits_;
@@ -235,6 +241,7 @@ int Renderer::Frame(const float* m) {
     q.unique_out = d_unique_;
     q.counts_out = d_counts_;
     RAYT_CUDA_TRY(launch_unique_from_bits(q, s_));
+    launches += 1 + (record ? 1 : 0);
     RAYT_CUDA_TRY(cudaEventRecord(ev_[2], s_));
     RAYT_CUDA_TRY(cudaMemcpyAsync(h_pass_, d_counters_, 3 * 4, cudaMemcpyDeviceToHost, s_));
     if (record) {
@@ -250,6 +257,7 @@ int Renderer::Frame(const float* m) {
     stats.rays_traced += active_prev;
     if (record) pass_words_.emplace_back(h_dense_, h_dense_ + total);
     const int active_now = h_pass_[1 + (it & 1)];
+    d2h += 3 * 4 + 2 * 4 + (int64_t)h_counts_[0] * 4;  // counters, counts, unique array
 
     // the reference always gives the frame one round of loading, then stops
     // on its wall-clock limit (gpu-ray-tracer.cpp:123-125)
@@ -285,6 +293,7 @@ int Renderer::Frame(const float* m) {
   p.active_in = d_active_[it & 1];
   p.n_active_in = d_counters_ + 1 + (it & 1);
   RAYT_CUDA_TRY(launch_finish(p, active_prev, s_));
+  if (active_prev > 0) ++launches;
   RAYT_CUDA_TRY(cudaStreamSynchronize(s_));
   if (stats.passes > 1 || stats.faults) {
     float up = 0;
@@ -295,6 +304,9 @@ int Renderer::Frame(const float* m) {
   stats.gpu_ms_upload = ms_up;
   stats.uploaded_blocks = (int)(cache_->stats().uploaded_blocks - uploaded0);
   stats.frame_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  stats.kernel_launches = launches + (int)(cache_->launches() - launches0);
+  stats.bytes_h2d = cache_->stats().bytes_h2d - h2d0;
+  stats.bytes_d2h = d2h;
   return RAYT_OK;
 }
 
@@ -402,6 +414,11 @@ int rayt_renderer_record_passes(rayt_renderer* r, int on) {
 int rayt_render_frame(rayt_renderer* r, const float m[16]) {
   if (!r || !m) return fail(RAYT_E_ARG, "rayt_render_frame: null argument");
   return R(r)->Frame(m);
+}
+int rayt_renderer_stream(rayt_renderer* r, void** stream) {
+  if (!r || !stream) return fail(RAYT_E_ARG, "null argument");
+  *stream = R(r)->stream();
+  return RAYT_OK;
 }
 int rayt_renderer_image(rayt_renderer* r, void** dev) {
   if (!r || !dev) return fail(RAYT_E_ARG, "null argument");
