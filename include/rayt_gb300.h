@@ -243,6 +243,21 @@ int rayt_scan_i32(int32_t* device_data, int n, void* stream);
 int rayt_feedback_unique(const int32_t* device_words, int n, int nodes_in_block,
                          int32_t* device_unique, int* unique_count, void* stream);
 
+/* No counterpart in the reference.  rayt_feedback_unique's computation for
+ * callers that cannot let the library allocate device memory (an application
+ * that owns all of HBM through its own allocator or reservation, or a frame
+ * loop that cannot absorb the device-wide wait of cudaFree).  It calls no
+ * cudaMalloc/cudaFree: its scratch is a fixed __device__ array of about
+ * 16.5 MiB that each GPU loading the library keeps until exit, sized for n up
+ * to RAYT_FEEDBACK_UNIQUE_NOALLOC_MAX_WORDS (larger n returns RAYT_E_LIMIT).
+ * All calls on a device share that array: calls whose GPU work overlaps race,
+ * so order them on one stream or synchronise in between.  The first call on a
+ * device looks up the array's address; make it before any stream capture.
+ * Returns after the result is on the device and *unique_count is set. */
+#define RAYT_FEEDBACK_UNIQUE_NOALLOC_MAX_WORDS (1 << 21)
+int rayt_feedback_unique_noalloc(const int32_t* device_words, int n, int nodes_in_block,
+                                 int32_t* device_unique, int* unique_count, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

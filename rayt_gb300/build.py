@@ -19,7 +19,7 @@ CU_FLAGS = ["-O3", "-std=c++17", "--fmad=false", "-prec-div=true", "-prec-sqrt=t
             "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "--expt-relaxed-constexpr"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math"]
 
-CU_SOURCES = ["trace.cu", "sort.cu", "upload.cu"]
+CU_SOURCES = ["trace.cu", "sort.cu", "upload.cu", "unique_noalloc.cu"]
 CXX_SOURCES = ["util.cpp", "tree.cpp", "cache.cpp", "renderer.cpp", "prims.cpp"]
 
 
