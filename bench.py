@@ -2,6 +2,9 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload c3|c1|c2]
 
+The default workload is c3, the configuration the Mrays/s-at-1080p metric is
+quoted on.
+
 A step is one frame of the plain per-frame path (RenderFrame: traversal
 passes, feedback unique, cache transaction with block streaming, finish) for
 the frame workloads, and one compaction + radix sort + unique of the feedback
@@ -48,9 +51,17 @@ def parse():
     ap.add_argument("--steps", type=int, default=0)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c1", choices=["c1", "c2", "c3"])
+    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU baseline sample")
-    return ap.parse_args()
+    ap.add_argument("--spheres", type=int, default=None, help="override the workload's sphere count")
+    ap.add_argument("--cache-mib", type=int, default=None, help="override the workload's cache size")
+    a = ap.parse_args()
+    if a.workload in WORKLOADS:
+        if a.spheres is not None:
+            WORKLOADS[a.workload]["spheres"] = a.spheres
+        if a.cache_mib is not None:
+            WORKLOADS[a.workload]["cache_bytes"] = a.cache_mib << 20
+    return a
 
 
 # ---------------------------------------------------------------------------

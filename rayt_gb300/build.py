@@ -17,7 +17,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # the reference's operation order.
 CU_FLAGS = ["-O3", "-std=c++17", "--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
             "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "--expt-relaxed-constexpr"]
-CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math"]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-pthread"]
 
 CU_SOURCES = ["trace.cu", "sort.cu", "upload.cu", "unique_noalloc.cu"]
 CXX_SOURCES = ["util.cpp", "tree.cpp", "cache.cpp", "renderer.cpp", "prims.cpp"]

@@ -49,9 +49,10 @@ class SphereTestSource {
 
   SphereTestNode GetRoot() { return SphereTestNode{0, {0, 0, 0}, {1, 1, 1}, 1}; }
 
-  std::vector<std::pair<int, SphereTestNode>> GetChildren(SphereTestNode& node) {
-    std::vector<std::pair<int, SphereTestNode>> res;
-    if (node.depth == max_depth_) return res;
+  // Children of `node` in slot order into slots[]/kids[] (room for 8).
+  int ChildrenInto(const SphereTestNode& node, int* slots, SphereTestNode* kids) const {
+    if (node.depth == max_depth_) return 0;
+    int k = 0;
     for (int ch = 0; ch < 8; ++ch) {
       SphereTestNode n;
       for (int a = 0; a < 3; ++a) {
@@ -62,17 +63,28 @@ class SphereTestSource {
       if (!Straddles(n.minp, n.maxp)) continue;
       n.depth = node.depth + 1;
       n.node_id = (int32_t)((uint32_t)node.node_id * 8u + (uint32_t)ch);
-      res.push_back(std::make_pair(ch, n));
+      slots[k] = ch;
+      kids[k++] = n;
     }
-    return res;
+    return k;
   }
-
-  void GetNodeData(SphereTestNode& node, const std::vector<std::pair<int, SphereTestNode*>>&,
-                   void* out) {
+  void NodeDataInto(SphereTestNode& node, const SphereTestNode* const*, int, void* out) const {
     unsigned char* d = static_cast<unsigned char*>(out);
     uint32_t id = (uint32_t)node.node_id;
     std::memcpy(d, &id, 4);
     d[4] = (unsigned char)(signed char)(node.node_id % 211);
+  }
+
+  std::vector<std::pair<int, SphereTestNode>> GetChildren(SphereTestNode& node) {
+    int slots[8];
+    SphereTestNode kids[8];
+    const int k = ChildrenInto(node, slots, kids);
+    std::vector<std::pair<int, SphereTestNode>> res;
+    for (int i = 0; i < k; ++i) res.push_back(std::make_pair(slots[i], kids[i]));
+    return res;
+  }
+  void GetNodeData(SphereTestNode& node, const std::vector<std::pair<int, SphereTestNode*>>&, void* out) {
+    NodeDataInto(node, nullptr, 0, out);
   }
 
  private:
@@ -151,9 +163,10 @@ class TerrainSource {
     return r;
   }
 
-  std::vector<std::pair<int, TerrainNode>> GetChildren(TerrainNode& node) {
-    std::vector<std::pair<int, TerrainNode>> res;
-    if (node.depth == p_.depth) return res;
+  // Children of `node` in slot order into slots[]/kids[] (room for 8).
+  int ChildrenInto(const TerrainNode& node, int* slots, TerrainNode* kids) const {
+    if (node.depth == p_.depth) return 0;
+    int k = 0;
     for (int ch = 0; ch < 8; ++ch) {
       TerrainNode c{};
       c.depth = node.depth + 1;
@@ -161,24 +174,39 @@ class TerrainSource {
       c.y = node.y * 2 + ((ch >> 1) & 1);
       c.z = node.z * 2 + ((ch >> 2) & 1);
       if (!Occupied(c)) continue;
-      res.push_back(std::make_pair(ch, c));
+      slots[k] = ch;
+      kids[k++] = c;
     }
-    return res;
+    return k;
   }
 
-  void GetNodeData(TerrainNode& node, const std::vector<std::pair<int, TerrainNode*>>& children,
-                   void* out) {
+  std::vector<std::pair<int, TerrainNode>> GetChildren(TerrainNode& node) {
+    int slots[8];
+    TerrainNode kids[8];
+    const int k = ChildrenInto(node, slots, kids);
+    std::vector<std::pair<int, TerrainNode>> res;
+    for (int i = 0; i < k; ++i) res.push_back(std::make_pair(slots[i], kids[i]));
+    return res;
+  }
+  void GetNodeData(TerrainNode& node, const std::vector<std::pair<int, TerrainNode*>>& children, void* out) {
+    const TerrainNode* kids[8];
+    for (size_t i = 0; i < children.size() && i < 8; ++i) kids[i] = children[i].second;
+    NodeDataInto(node, kids, (int)children.size(), out);
+  }
+
+  // Node data from the children (in slot order); kids may be null when n == 0.
+  void NodeDataInto(TerrainNode& node, const TerrainNode* const* kids, int n, void* out) const {
     float nx = 0, ny = 0, nz = 0;
-    if (children.empty()) {
+    if (n == 0) {
       LeafData(node);
     } else {
       float cr = 0, cg = 0, cb = 0;
-      for (size_t i = 0; i < children.size(); ++i) {
-        const TerrainNode* c = children[i].second;
+      for (int i = 0; i < n; ++i) {
+        const TerrainNode* c = kids[i];
         nx = nx + c->normal[0]; ny = ny + c->normal[1]; nz = nz + c->normal[2];
         cr = cr + c->color[0]; cg = cg + c->color[1]; cb = cb + c->color[2];
       }
-      float inv = 1.0f / (float)children.size();
+      float inv = 1.0f / (float)n;
       node.color[0] = cr * inv; node.color[1] = cg * inv; node.color[2] = cb * inv;
       node.normal[0] = nx; node.normal[1] = ny; node.normal[2] = nz;
     }

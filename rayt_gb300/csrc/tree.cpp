@@ -11,6 +11,8 @@
 //    double precision; see Inverse() below for why it is not bit-identical.
 #include <algorithm>
 #include <cerrno>
+#include <cstdlib>
+#include <thread>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -177,6 +179,15 @@ M4 Inverse(const M4& a) {
 }
 }  // namespace
 
+// Builder threads: RAYT_BUILD_THREADS if set, else every hardware thread.  The
+// file is the same for any thread count.
+int build_threads() {
+  const char* e = std::getenv("RAYT_BUILD_THREADS");
+  if (e && std::atoi(e) > 0) return std::atoi(e);
+  const unsigned hw = std::thread::hardware_concurrency();
+  return hw ? (int)hw : 1;
+}
+
 }  // namespace rayt
 
 using rayt::fail;
@@ -226,7 +237,7 @@ int rayt_build_sphere_test(const char* path, float cx, float cy, float cz, float
   try {
     rayt_scene::SphereTestSource src(cx, cy, cz, radius, depth);
     std::vector<rayt_build::Channel> ch{{4, "node index"}, {1, "node index % 211"}};
-    rayt_build::BlockBuilder<rayt_scene::SphereTestSource> b(path, nodes_in_block, ch, &src);
+    rayt_build::BlockBuilder<rayt_scene::SphereTestSource> b(path, nodes_in_block, ch, &src, rayt::build_threads());
     uint32_t n = b.Build();
     if (blocks_out) *blocks_out = n;
   } catch (const std::exception& e) {
@@ -252,7 +263,7 @@ int rayt_build_terrain(const char* path, const rayt_terrain_params* prm, int nod
     p.max_radius = prm->max_radius;
     rayt_scene::TerrainSource src(p);
     std::vector<rayt_build::Channel> ch{{4, "normals"}, {4, "colors"}};
-    rayt_build::BlockBuilder<rayt_scene::TerrainSource> b(path, nodes_in_block, ch, &src);
+    rayt_build::BlockBuilder<rayt_scene::TerrainSource> b(path, nodes_in_block, ch, &src, rayt::build_threads());
     uint32_t n = b.Build();
     if (blocks_out) *blocks_out = n;
     if (nodes_out) *nodes_out = b.nodes();
