@@ -19,10 +19,96 @@
 // kernel - instead of per-channel and per-pointer clEnqueueWriteBuffer calls.
 #include "cache.h"
 
+#include <atomic>
 #include <chrono>
+#include <condition_variable>
+#include <cstdlib>
 #include <cstring>
+#include <functional>
+#include <mutex>
+#include <thread>
 
 namespace rayt {
+
+// Threads that read staged blocks from the file in parallel.  Run() returns
+// only after every item is done and every worker has left the job, so the
+// next Run() can reset the shared counters.
+class Cache::ReadPool {
+ public:
+  explicit ReadPool(int threads) {
+    for (int t = 0; t < threads; ++t) workers_.emplace_back([this] { Loop(); });
+  }
+  ~ReadPool() {
+    {
+      std::lock_guard<std::mutex> lock(mu_);
+      quit_ = true;
+    }
+    cv_.notify_all();
+    for (auto& w : workers_) w.join();
+  }
+  // Runs fn(0..n-1) on the pool and the calling thread.
+  void Run(int n, const std::function<void(int)>& fn) {
+    if (n <= 0) return;
+    {
+      std::lock_guard<std::mutex> lock(mu_);
+      fn_ = &fn;
+      n_ = n;
+      next_.store(0);
+      done_ = 0;
+      ++gen_;
+    }
+    cv_.notify_all();
+    const int mine = Work(fn, n);
+    std::unique_lock<std::mutex> lock(mu_);
+    done_ += mine;
+    done_cv_.wait(lock, [this] { return done_ == n_ && active_ == 0; });
+    fn_ = nullptr;
+  }
+
+ private:
+  std::vector<std::thread> workers_;
+  std::mutex mu_;
+  std::condition_variable cv_, done_cv_;
+  const std::function<void(int)>* fn_ = nullptr;
+  int n_ = 0, done_ = 0, active_ = 0;
+  uint64_t gen_ = 0;
+  std::atomic<int> next_{0};
+  bool quit_ = false;
+
+  int Work(const std::function<void(int)>& fn, int n) {
+    int finished = 0;
+    for (;;) {
+      const int i = next_.fetch_add(1);
+      if (i >= n) break;
+      fn(i);
+      ++finished;
+    }
+    return finished;
+  }
+  void Loop() {
+    uint64_t seen = 0;
+    for (;;) {
+      const std::function<void(int)>* fn;
+      int n;
+      {
+        std::unique_lock<std::mutex> lock(mu_);
+        cv_.wait(lock, [&] { return quit_ || (gen_ != seen && fn_); });
+        if (quit_) return;
+        seen = gen_;
+        fn = fn_;
+        n = n_;
+        ++active_;
+      }
+      const int finished = Work(*fn, n);
+      {
+        std::lock_guard<std::mutex> lock(mu_);
+        done_ += finished;
+        --active_;
+      }
+      done_cv_.notify_all();
+    }
+  }
+};
 
 namespace {
 inline uint32_t CacheLink(uint32_t mask, bool fault, bool dup, bool far_flag, uint32_t ptr) {
@@ -34,6 +120,7 @@ constexpr size_t kStageBytes = 32u << 20;  // per half
 }  // namespace
 
 Cache::~Cache() {
+  delete pool_;
   if (stream_) cudaStreamSynchronize(stream_);
   for (uint8_t* p : d_chan_) cudaFree(p);
   cudaFree(d_far_);
@@ -44,6 +131,8 @@ Cache::~Cache() {
   cudaFreeHost(h_slots_);
   cudaFreeHost(h_patches_);
   for (auto& e : stage_free_)
+    if (e) cudaEventDestroy(e);
+  for (auto& e : patch_free_)
     if (e) cudaEventDestroy(e);
   if (stream_) cudaStreamDestroy(stream_);
 }
@@ -70,18 +159,26 @@ int Cache::Init(Tree* tree, int max_blocks) {
   if (cudaMalloc(&d_far_, (size_t)max_blocks_ * 8 * 4) != cudaSuccess) return fail(RAYT_E_OOM, "far pointer allocation failed");
   RAYT_CUDA_TRY(cudaMemsetAsync(d_far_, 0, (size_t)max_blocks_ * 8 * 4, stream_));
 
-  stride_ = ((size_t)tree->info.content_bytes + 15) & ~(size_t)15;
-  stage_cap_ = (int)std::max<size_t>(kStageBlocksMin, kStageBytes / stride_);
-  if (cudaHostAlloc(&h_stage_, stride_ * stage_cap_ * 2, cudaHostAllocDefault) != cudaSuccess ||
-      cudaMalloc(&d_stage_, stride_ * stage_cap_ * 2) != cudaSuccess ||
+  area_ = ((size_t)tree->info.content_bytes + 80 + 15) & ~(size_t)15;
+  stage_cap_ = (int)std::max<size_t>(kStageBlocksMin, kStageBytes / area_);
+  if (cudaHostAlloc(&h_stage_, area_ * stage_cap_ * 2, cudaHostAllocDefault) != cudaSuccess ||
+      cudaMalloc(&d_stage_, area_ * stage_cap_ * 2) != cudaSuccess ||
       cudaHostAlloc(&h_slots_, sizeof(int) * stage_cap_ * 2, cudaHostAllocDefault) != cudaSuccess ||
       cudaMalloc(&d_slots_, sizeof(int) * stage_cap_ * 2) != cudaSuccess)
     return fail(RAYT_E_OOM, "staging allocation failed");
   for (auto& e : stage_free_) RAYT_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  for (auto& e : patch_free_) RAYT_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  meta_.resize((size_t)stage_cap_ * 2);
   patch_cap_ = stage_cap_ * 32 + 64;
   if (cudaHostAlloc(&h_patches_, sizeof(Patch) * patch_cap_ * 2, cudaHostAllocDefault) != cudaSuccess ||
       cudaMalloc(&d_patches_, sizeof(Patch) * patch_cap_ * 2) != cudaSuccess)
     return fail(RAYT_E_OOM, "patch buffer allocation failed");
+  {
+    const char* e = std::getenv("RAYT_IO_THREADS");
+    int threads = e && std::atoi(e) > 0 ? std::atoi(e) : (int)std::thread::hardware_concurrency();
+    threads = std::max(1, std::min(threads, 16));
+    pool_ = new ReadPool(threads - 1);  // the calling thread reads too
+  }
 
   slots_.resize((size_t)max_blocks_);
   block_slot_.assign(tree->info.blocks_count, -1);
@@ -172,20 +269,24 @@ void Cache::AddPatch(bool far_buffer, uint32_t index, uint32_t value) {
   if (far_buffer) ++stats_.far_pointer_writes;
 }
 
-int Cache::Flush() {
-  if (staged_ == 0 && patches_.empty()) return RAYT_OK;
+// Uploads positions [batch_begin_, end) of the current half (slot -1 =
+// staged but not placed: skipped by the kernel), then the batch's patches.
+int Cache::FlushTo(int end) {
+  if (end <= batch_begin_ && patches_.empty()) return RAYT_OK;
   const int h = half_;
-  uint8_t* hs = h_stage_ + stride_ * stage_cap_ * h;
-  uint8_t* ds = d_stage_ + stride_ * stage_cap_ * h;
-  if (staged_ > 0) {
-    RAYT_CUDA_TRY(cudaMemcpyAsync(ds, hs, stride_ * staged_, cudaMemcpyHostToDevice, stream_));
-    RAYT_CUDA_TRY(cudaMemcpyAsync(d_slots_ + stage_cap_ * h, h_slots_ + stage_cap_ * h, sizeof(int) * staged_,
-                                  cudaMemcpyHostToDevice, stream_));
+  if (end > batch_begin_) {
+    const size_t first = (size_t)stage_cap_ * h + batch_begin_;
+    const int n = end - batch_begin_;
+    uint8_t* hs = h_stage_ + area_ * first;
+    uint8_t* ds = d_stage_ + area_ * first;
+    RAYT_CUDA_TRY(cudaMemcpyAsync(ds, hs, area_ * n, cudaMemcpyHostToDevice, stream_));
+    RAYT_CUDA_TRY(cudaMemcpyAsync(d_slots_ + first, h_slots_ + first, sizeof(int) * n, cudaMemcpyHostToDevice,
+                                  stream_));
     UploadParams up{};
-    up.stage = ds;
-    up.stride = stride_;
-    up.slots = d_slots_ + stage_cap_ * h;
-    up.blocks = staged_;
+    up.stage = ds + 80;
+    up.stride = area_;
+    up.slots = d_slots_ + first;
+    up.blocks = n;
     up.nodes_in_block = nib_;
     up.channels = (int)d_chan_.size();
     for (int c = 0; c < up.channels; ++c) {
@@ -194,30 +295,40 @@ int Cache::Flush() {
     }
     RAYT_CUDA_TRY(launch_upload(up, stream_));
     ++launches_;
-    stats_.bytes_h2d += (int64_t)(stride_ * staged_);
+    stats_.bytes_h2d += (int64_t)(area_ * n);
   }
   size_t done = 0;
   while (done < patches_.size()) {
     const size_t n = std::min(patches_.size() - done, (size_t)patch_cap_);
-    Patch* hp = h_patches_ + (size_t)patch_cap_ * h;
-    Patch* dp = d_patches_ + (size_t)patch_cap_ * h;
-    // the pinned half is reused only after its previous copy finished
-    RAYT_CUDA_TRY(cudaEventSynchronize(stage_free_[h]));
+    const int ph = patch_half_;
+    Patch* hp = h_patches_ + (size_t)patch_cap_ * ph;
+    Patch* dp = d_patches_ + (size_t)patch_cap_ * ph;
+    // a pinned patch half is refilled only after its previous copy finished
+    RAYT_CUDA_TRY(cudaEventSynchronize(patch_free_[ph]));
     std::memcpy(hp, patches_.data() + done, n * sizeof(Patch));
     RAYT_CUDA_TRY(cudaMemcpyAsync(dp, hp, n * sizeof(Patch), cudaMemcpyHostToDevice, stream_));
     RAYT_CUDA_TRY(launch_patches(dp, (int)n, reinterpret_cast<uint32_t*>(d_chan_[0]), d_far_, stream_));
+    RAYT_CUDA_TRY(cudaEventRecord(patch_free_[ph], stream_));
+    patch_half_ ^= 1;
     ++launches_;
     stats_.bytes_h2d += (int64_t)(n * sizeof(Patch));
     done += n;
-    if (done < patches_.size()) RAYT_CUDA_TRY(cudaEventRecord(stage_free_[h], stream_));
   }
-  RAYT_CUDA_TRY(cudaEventRecord(stage_free_[h], stream_));
   patches_.clear();
   patch_at_.clear();
-  staged_ = 0;
-  half_ ^= 1;
+  batch_begin_ = std::max(batch_begin_, end);
   ++epoch_;
-  // the next batch writes into the other half once its last copy is done
+  return RAYT_OK;
+}
+
+// Flushes what is staged and continues in the other half once that half's
+// last copies have finished.
+int Cache::NextHalf() {
+  int rc = FlushTo(staged_);
+  if (rc != RAYT_OK) return rc;
+  RAYT_CUDA_TRY(cudaEventRecord(stage_free_[half_], stream_));
+  half_ ^= 1;
+  staged_ = batch_begin_ = 0;
   RAYT_CUDA_TRY(cudaEventSynchronize(stage_free_[half_]));
   return RAYT_OK;
 }
@@ -249,21 +360,84 @@ int Cache::Unload() {
   return s;
 }
 
-// LoadBlock + UploadBlock (gpu-octree-cache.cpp:102-234); with a queue, fault
-// children are appended for InitialFillCache's breadth-first order.
-int Cache::LoadAndUpload(int block, bool scan_children, std::vector<int>* queue) {
+// LoadBlock (stored-octree-loader.cpp:31-58) into staging position `pos` of
+// the current half, with the checks and the fault-link scan UploadBlock needs.
+// Safe to run on several threads for different positions.
+int Cache::ReadOne(int pos, int block) {
+  Staged& m = meta_[(size_t)stage_cap_ * half_ + pos];
+  m.block = block;
+  m.rc = RAYT_OK;
+  m.faults.clear();
+  uint8_t* area = h_stage_ + area_ * ((size_t)stage_cap_ * half_ + pos);
   const size_t content = tree_->info.content_bytes;
-  if (staged_ == stage_cap_) {
-    int rc = Flush();
-    if (rc != RAYT_OK) return rc;
+  const int64_t off = (int64_t)tree_->info.header_bytes + (int64_t)tree_->info.block_stride * (uint32_t)block;
+  if (!tree_->Read(off, 76 + content, area + 4)) {
+    m.rc = RAYT_E_IO;
+    m.err = "block read failed";
+    return m.rc;
   }
-  uint8_t* dst = h_stage_ + stride_ * stage_cap_ * half_ + stride_ * staged_;
-  rayt_block_header hdr;
+  const uint8_t* raw = area + 4;
+  rayt_block_header& hdr = m.hdr;
+  std::memcpy(&hdr.block_index, raw, 4);
+  std::memcpy(&hdr.parent_block_index, raw + 4, 4);
+  std::memcpy(&hdr.roots_count, raw + 8, 4);
+  for (int i = 0; i < 8; ++i) {
+    std::memcpy(&hdr.roots[i].parent_pointer_index, raw + 12 + 8 * i, 2);
+    std::memcpy(&hdr.roots[i].pointed_child_index, raw + 14 + 8 * i, 2);
+    std::memcpy(&hdr.roots[i].parent_pointer_value, raw + 16 + 8 * i, 4);
+  }
+  auto bad = [&m](const char* why) {
+    m.rc = RAYT_E_FORMAT;
+    m.err = why;
+    return m.rc;
+  };
+  if (hdr.roots_count < 1 || hdr.roots_count > 8) return bad("block has an invalid root count");
+  const uint32_t blocks = tree_->info.blocks_count;
+  if (hdr.parent_block_index != kRootParent) {
+    for (uint32_t i = 0; i < hdr.roots_count; ++i) {
+      const rayt_block_root& r = hdr.roots[i];
+      const uint32_t pv = r.parent_pointer_value;
+      if (r.parent_pointer_index >= nib_ || r.pointed_child_index >= nib_ ||
+          (((pv >> 8) & 1u) && (pv & 255u) && (pv >> 11) >= blocks))
+        return bad("block root record is out of range");
+    }
+  }
+  const uint32_t* links = reinterpret_cast<const uint32_t*>(area + 80);
+  for (int n = 0; n < nib_; ++n) {
+    const uint32_t l = links[n], mask = l & 255u, ptr = l >> 11;
+    if (!mask) continue;
+    if (!((l >> 8) & 1u)) {
+      // children inside the block: every one of them must be a node of the block
+      if (ptr + (uint32_t)__builtin_popcount(mask) > (uint32_t)nib_)
+        return bad("child link points past the end of its block");
+      continue;
+    }
+    if (ptr >= blocks) return bad("fault link points past the last block");
+    m.faults.push_back(ptr);
+  }
+  return RAYT_OK;
+}
+
+// Reads blocks[0..n) into positions [staged_, staged_ + n) in parallel.
+int Cache::Prefetch(const int* blocks, int n) {
+  const int first = staged_;
   const auto t0 = std::chrono::steady_clock::now();
-  int rc = tree_->LoadBlock((uint32_t)block, &hdr, dst);
+  pool_->Run(n, [&](int i) { ReadOne(first + i, blocks[i]); });
   stats_.io_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-  if (rc != RAYT_OK) return rc;
-  stats_.bytes_read += (int64_t)content + 76;
+  for (int i = 0; i < n; ++i) h_slots_[(size_t)stage_cap_ * half_ + first + i] = -1;
+  staged_ += n;
+  return RAYT_OK;
+}
+
+// UploadBlock (gpu-octree-cache.cpp:102-234) for the block staged at `pos`;
+// with a queue, its fault children are appended in InitialFillCache's
+// breadth-first order.
+int Cache::Place(int pos, std::vector<int>* queue) {
+  Staged& m = meta_[(size_t)stage_cap_ * half_ + pos];
+  if (m.rc != RAYT_OK) return fail(m.rc, "cache: " + m.err);
+  const int block = m.block;
+  const rayt_block_header& hdr = m.hdr;
+  stats_.bytes_read += (int64_t)tree_->info.content_bytes + 76;
   const bool is_root = hdr.parent_block_index == kRootParent;
   const int root_child = hdr.roots[0].pointed_child_index;
   if (!is_root && parent_slot_[block] < 0) return fail(RAYT_E_STATE, "cache: parent of a requested block is not resident");
@@ -278,35 +452,21 @@ int Cache::LoadAndUpload(int block, bool scan_children, std::vector<int>* queue)
   }
   if (touched_[s] == epoch_) {
     // The slot was written or patched earlier in this batch: a batch applies
-    // all block contents before all patches, so submit what is staged (with
-    // the eviction's restore patches) first, then stage this block anew.
-    std::vector<uint8_t> keep(dst, dst + content);
-    rc = Flush();
+    // all block contents before all patches, so submit the batch before this
+    // position (with the eviction's restore patches) first.
+    int rc = FlushTo(pos);
     if (rc != RAYT_OK) return rc;
-    dst = h_stage_ + stride_ * stage_cap_ * half_ + stride_ * staged_;
-    std::memcpy(dst, keep.data(), content);
   }
-  h_slots_[stage_cap_ * half_ + staged_] = s;
-  ++staged_;
+  h_slots_[(size_t)stage_cap_ * half_ + pos] = s;
   touched_[s] = epoch_;
 
   Slot& info = slots_[s];
-  const uint32_t* links = reinterpret_cast<const uint32_t*>(dst);
-  for (int n = 0; n < nib_; ++n) {
-    const uint32_t l = links[n], mask = l & 255u, fault = (l >> 8) & 1u, ptr = l >> 11;
-    if (!mask) continue;
-    if (!fault) {
-      // children inside the block: every one of them must be a node of the block
-      if (ptr + (uint32_t)__builtin_popcount(mask) > (uint32_t)nib_)
-        return fail(RAYT_E_FORMAT, "child link points past the end of its block");
-      continue;
-    }
-    if (ptr >= tree_->info.blocks_count) return fail(RAYT_E_FORMAT, "fault link points past the last block");
+  for (uint32_t ptr : m.faults) {
     if (parent_slot_[ptr] < 0) {
       parent_slot_[ptr] = s;
       info.children.push_back((int)ptr);
     }
-    if (scan_children && queue) queue->push_back((int)ptr);
+    if (queue) queue->push_back((int)ptr);
   }
   ++stats_.uploaded_blocks;
 
@@ -317,9 +477,6 @@ int Cache::LoadAndUpload(int block, bool scan_children, std::vector<int>* queue)
     for (uint32_t i = 0; i < hdr.roots_count; ++i) {
       const rayt_block_root& r = hdr.roots[i];
       const uint32_t pv = r.parent_pointer_value;
-      if (r.parent_pointer_index >= nib_ || r.pointed_child_index >= nib_ ||
-          (((pv >> 8) & 1u) && (pv & 255u) && (pv >> 11) >= tree_->info.blocks_count))
-        return fail(RAYT_E_FORMAT, "block root record is out of range");
       info.ptr_index[i] = r.parent_pointer_index;
       info.ptr_value[i] = r.parent_pointer_value;
       const int64_t absolute = (int64_t)s * nib_ + r.pointed_child_index;
@@ -349,17 +506,34 @@ int Cache::LoadAndUpload(int block, bool scan_children, std::vector<int>* queue)
 }
 
 // InitialFillCache (gpu-octree-cache-manager.cpp:60-108)
+// The queue holds a block once per fault link that names it (often dozens of
+// times); the reference skips an entry whose block is already in the cache
+// when it pops it.  Here the next chunk takes the first occurrence of each
+// block not yet loaded, reads the chunk in parallel and loads it in order -
+// the same blocks in the same order.
 int Cache::InitialFill() {
   std::vector<int> queue{(int)tree_->info.root_block_index};
+  std::vector<uint8_t> taken(tree_->info.blocks_count, 0);
+  std::vector<int> chunk;
   size_t head = 0;
+  int rc = RAYT_OK;
   while (first_free_ < max_blocks_ && head < queue.size()) {
-    const int index = queue[head++];
-    if (block_slot_[index] >= 0) continue;
-    int rc = LoadAndUpload(index, true, &queue);
-    if (rc != RAYT_OK) return rc;
+    if (staged_ == stage_cap_ && (rc = NextHalf()) != RAYT_OK) return rc;
+    const int room = std::min(stage_cap_ - staged_, max_blocks_ - first_free_);
+    chunk.clear();
+    while (head < queue.size() && (int)chunk.size() < room) {
+      const int b = queue[head++];
+      if (taken[b] || block_slot_[b] >= 0) continue;
+      taken[b] = 1;
+      chunk.push_back(b);
+    }
+    if (chunk.empty()) break;
+    const int first = staged_;
+    if ((rc = Prefetch(chunk.data(), (int)chunk.size())) != RAYT_OK) return rc;
+    for (int i = 0; i < (int)chunk.size() && first_free_ < max_blocks_; ++i)
+      if ((rc = Place(first + i, &queue)) != RAYT_OK) return rc;
   }
-  int rc = Flush();
-  if (rc != RAYT_OK) return rc;
+  if ((rc = FlushTo(staged_)) != RAYT_OK) return rc;
   RAYT_CUDA_TRY(cudaStreamSynchronize(stream_));
   return RAYT_OK;
 }
@@ -399,16 +573,32 @@ int Cache::RequestBlock(int block) {
   return RAYT_OK;
 }
 // EndRequestTransaction (gpu-octree-cache-manager.cpp:150-194)
+// The pending blocks are read a chunk at a time in parallel (reads have no
+// side effects), then placed one by one in request order until the
+// transaction fills the cache, exactly as the reference's loop does.
 int Cache::EndTransaction() {
   if (!in_transaction_) return fail(RAYT_E_STATE, "no open transaction");
   int rc = RAYT_OK;
-  for (size_t i = 0; i < pending_.size(); ++i) {
+  size_t i = 0;
+  bool filled = false;
+  while (rc == RAYT_OK && !filled && i < pending_.size()) {
     if (TransactionFilled()) break;
-    rc = LoadAndUpload(pending_[i], false, nullptr);
-    if (rc != RAYT_OK) break;
+    if (staged_ == stage_cap_ && (rc = NextHalf()) != RAYT_OK) break;
+    const int n = (int)std::min<size_t>((size_t)(stage_cap_ - staged_), pending_.size() - i);
+    const int first = staged_;
+    if ((rc = Prefetch(pending_.data() + i, n)) != RAYT_OK) break;
+    i += n;
+    for (int k = 0; k < n; ++k) {
+      if (TransactionFilled()) {
+        filled = true;
+        break;
+      }
+      if (block_slot_[meta_[(size_t)stage_cap_ * half_ + first + k].block] >= 0) continue;
+      if ((rc = Place(first + k, nullptr)) != RAYT_OK) break;
+    }
   }
   pending_.clear();
-  const int frc = Flush();
+  const int frc = FlushTo(staged_);
   in_transaction_ = false;
   DropMarker(kTransaction);
   return rc != RAYT_OK ? rc : frc;

@@ -77,21 +77,36 @@ class Cache {
   std::vector<int> pending_;
   bool in_session_ = false, in_transaction_ = false;
 
-  // upload batch
-  uint8_t* h_stage_ = nullptr;   // pinned, stage_cap_ blocks per half, two halves
+  // Block staging: two halves of stage_cap_ positions in pinned host memory
+  // and in device memory.  A position holds one block record read with a
+  // single pread: the 76-byte header at +4 and the content at +80, so the
+  // content is 16-byte aligned.  Positions [batch_begin_, staged_) of the
+  // current half form the batch the next flush uploads.
+  struct Staged {
+    int block = -1;
+    int rc = RAYT_OK;
+    std::string err;
+    rayt_block_header hdr{};
+    std::vector<uint32_t> faults;  // fault-link targets, in node order
+  };
+  uint8_t* h_stage_ = nullptr;
   uint8_t* d_stage_ = nullptr;
-  int stage_cap_ = 0, half_ = 0, staged_ = 0;
-  size_t stride_ = 0;            // staging stride: content bytes rounded up to 16
+  size_t area_ = 0;              // bytes per staging position
+  int stage_cap_ = 0, half_ = 0, staged_ = 0, batch_begin_ = 0;
   cudaEvent_t stage_free_[2] = {nullptr, nullptr};
-  int* h_slots_ = nullptr;       // pinned, per half
+  std::vector<Staged> meta_;     // per position, both halves
+  int* h_slots_ = nullptr;       // pinned, per position (-1: staged but not placed)
   int* d_slots_ = nullptr;
   std::vector<Patch> patches_;
   std::unordered_map<uint32_t, int> patch_at_;
-  Patch* h_patches_ = nullptr;   // pinned
+  Patch* h_patches_ = nullptr;   // pinned, two halves
   Patch* d_patches_ = nullptr;
-  int patch_cap_ = 0;
+  int patch_cap_ = 0, patch_half_ = 0;
+  cudaEvent_t patch_free_[2] = {nullptr, nullptr};
   std::vector<int> touched_;     // batch epoch in which a slot was written or patched
   int epoch_ = 1;
+  class ReadPool;
+  ReadPool* pool_ = nullptr;
 
   rayt_cache_stats stats_{};
   int64_t launches_ = 0;   // upload and patch kernels launched
@@ -104,10 +119,13 @@ class Cache {
   void InsertMarker(int k);
   void DropMarker(int k);
 
-  int LoadAndUpload(int block, bool scan_children_to_queue, std::vector<int>* queue);
+  int ReadOne(int pos, int block);
+  int Prefetch(const int* blocks, int n);
+  int Place(int pos, std::vector<int>* queue);
   int Unload();
   void AddPatch(bool far_buffer, uint32_t index, uint32_t value);
-  int Flush();
+  int FlushTo(int end);
+  int NextHalf();
 };
 
 }  // namespace rayt

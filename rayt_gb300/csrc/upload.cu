@@ -22,6 +22,7 @@ __global__ void __launch_bounds__(kThreads) upload_kernel(const __grid_constant_
   const int b = blockIdx.x;
   const size_t nib = (size_t)p.nodes_in_block;
   const uint8_t* src = p.stage + (size_t)b * p.stride;
+  if (p.slots[b] < 0) return;  // staged but not placed (read ahead, then not needed)
   const size_t slot = (size_t)p.slots[b];
 
   // channel 0: node links, stored format -> cache format
