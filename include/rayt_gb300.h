@@ -196,8 +196,36 @@ int rayt_renderer_stream(rayt_renderer* r, void** stream);
 /* GPURayTracer::out_image(): RGBA8 frame, row 0 at the bottom. */
 int rayt_renderer_image(rayt_renderer* r, void** device_rgba);
 int rayt_renderer_read_image(rayt_renderer* r, void* host_rgba, size_t bytes);
-/* Dense feedback words of pass `pass` of the last frame (recording on). */
+/* Dense feedback words of pass `pass` of the last frame (recording on); views
+ * follow one another in view order. */
 int rayt_renderer_pass_words(rayt_renderer* r, int pass, int32_t* host_words, size_t count);
+
+/* Batched form (no counterpart in the reference, which renders one view per
+ * RenderFrame).  A renderer over n_views views (1..512) of any sizes; each
+ * frame traces all views in the same persistent launches and one cache
+ * session, so their feedback is merged into one request list per pass and the
+ * pass loop ends as RenderFrame's does.  Once the cache holds every block the
+ * views touch, each view's image equals a one-view frame of that camera. */
+int rayt_renderer_create_views(rayt_cache* cache, int n_views, const int* widths, const int* heights,
+                               rayt_renderer** out);
+/* One frame of every view; view_proj_inv holds n_views matrices of 16 floats. */
+int rayt_render_views(rayt_renderer* r, const float* view_proj_inv, int n_views);
+int rayt_renderer_view_count(const rayt_renderer* r);
+int rayt_renderer_view_image(rayt_renderer* r, int view, void** device_rgba);
+int rayt_renderer_read_view_image(rayt_renderer* r, int view, void* host_rgba, size_t bytes);
+/* Traversal launch shape: a warp's 32 first-pass rays cover a
+ * (1 << tile_w_log2) x (32 >> tile_w_log2) pixel tile.  refill = 32: one
+ * thread per ray over a grid covering all rays.  refill < 32: a persistent
+ * kernel (ctas_per_sm resident CTAs per SM, 0 = as many as fit) whose warps
+ * take rays from a work counter, stop their rays every step_budget traversal
+ * iterations and hand new rays to idle lanes once at least `refill` of them
+ * are idle.  Default {2, 32, 0, 16}.  Results do not depend on the shape. */
+int rayt_renderer_set_launch_shape(rayt_renderer* r, int tile_w_log2, int refill, int ctas_per_sm, int step_budget);
+int rayt_renderer_get_launch_shape(const rayt_renderer* r, int shape[4]);
+/* Times first passes over the given view matrices (as rayt_renderer_time_pass)
+ * for every launch shape of a fixed candidate set, keeps the fastest and
+ * returns it in best ({tile_w_log2, refill, ctas_per_sm, step_budget}). */
+int rayt_renderer_autotune(rayt_renderer* r, const float* view_proj_inv, int reps, int best[4]);
 
 typedef struct {
   int passes;                /* tracing passes of the last frame */
@@ -215,14 +243,14 @@ typedef struct {
 } rayt_frame_stats;
 int rayt_renderer_stats(const rayt_renderer* r, rayt_frame_stats* out);
 
-/* Traces one pass from view_proj_inv against the cache as it is (no feedback,
- * no uploads) and counts node-link and far-pointer fetches: the algorithmic
- * byte count of the traversal roofline.  counts = {rays, link fetches, far
- * fetches, iterations, hits, faults}. */
-int rayt_renderer_count_fetches(rayt_renderer* r, const float view_proj_inv[16], int64_t counts[6]);
+/* Traces one pass from view_proj_inv (one matrix per view) against the cache
+ * as it is (no feedback, no uploads) and counts node-link and far-pointer
+ * fetches: the algorithmic byte count of the traversal roofline.  counts =
+ * {rays, link fetches, far fetches, iterations, hits, faults}. */
+int rayt_renderer_count_fetches(rayt_renderer* r, const float* view_proj_inv, int64_t counts[6]);
 /* Times `reps` back-to-back first passes (ray setup + traversal + shading) on
  * the renderer's stream with CUDA events; returns milliseconds per pass. */
-int rayt_renderer_time_pass(rayt_renderer* r, const float view_proj_inv[16], int reps, float* ms_per_pass);
+int rayt_renderer_time_pass(rayt_renderer* r, const float* view_proj_inv, int reps, float* ms_per_pass);
 
 /* ------------------------------------------------------------------------ */
 /* Feedback primitives on device arrays of int32. */

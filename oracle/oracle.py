@@ -34,6 +34,8 @@ def lib():
             "oracle_cache_read": (i32, [vp, i32, vp, C.c_longlong]),
             "oracle_cache_counters": (None, [vp, C.POINTER(C.c_longlong)]),
             "oracle_renderer_create": (vp, [vp, i32, i32, C.c_float, C.c_double, i32]),
+            "oracle_renderer_create_views": (vp, [vp, i32, C.POINTER(i32), C.POINTER(i32), C.c_float, C.c_double, i32]),
+            "oracle_frame_view_image": (i32, [vp, i32, vp]),
             "oracle_renderer_destroy": (None, [vp]),
             "oracle_renderer_record": (None, [vp, i32]),
             "oracle_render_frame": (i32, [vp, C.POINTER(C.c_float)]),
@@ -61,7 +63,7 @@ def _m(mat):
 class OracleScene:
     """Block file + cache + renderer on the CPU (reference semantics)."""
 
-    def __init__(self, path, max_blocks=0, width=0, height=0, lod=1.0, time_limit=1e30, max_passes=0):
+    def __init__(self, path, max_blocks=0, width=0, height=0, lod=1.0, time_limit=1e30, max_passes=0, views=None):
         L = lib()
         self.tree = L.oracle_tree_open(os.fsencode(path))
         if not self.tree:
@@ -72,7 +74,17 @@ class OracleScene:
         self.nib = L.oracle_tree_nib(self.tree)
         self.max_blocks = L.oracle_cache_max_blocks(self.cache)
         self.w, self.h = width, height
-        self.r = L.oracle_renderer_create(self.cache, width, height, lod, time_limit, max_passes) if width else None
+        self.views = None
+        if views:
+            # several views traced together per frame (the batched form)
+            self.views = [(int(a), int(b)) for a, b in views]
+            n = len(self.views)
+            ws = (C.c_int * n)(*[a for a, _ in self.views])
+            hs = (C.c_int * n)(*[b for _, b in self.views])
+            self.w, self.h = self.views[0]
+            self.r = L.oracle_renderer_create_views(self.cache, n, ws, hs, lod, time_limit, max_passes)
+        else:
+            self.r = L.oracle_renderer_create(self.cache, width, height, lod, time_limit, max_passes) if width else None
 
     def root(self):
         return lib().oracle_cache_root(self.cache)
@@ -89,8 +101,21 @@ class OracleScene:
         lib().oracle_frame_image(self.r, img.ctypes.data)
         return n, img
 
+    def render_views(self, mats):
+        """One frame of every view; returns (passes, [image per view])."""
+        m = np.ascontiguousarray(np.asarray(mats, np.float32).reshape(len(self.views) * 16))
+        n = lib().oracle_render_frame(self.r, m.ctypes.data_as(C.POINTER(C.c_float)))
+        if n < 0:
+            raise RuntimeError("oracle: " + lib().oracle_last_error().decode())
+        imgs = []
+        for v, (w, h) in enumerate(self.views):
+            img = np.zeros((h, w, 4), np.uint8)
+            lib().oracle_frame_view_image(self.r, v, img.ctypes.data)
+            imgs.append(img)
+        return n, imgs
+
     def pass_words(self, i):
-        out = np.zeros(self.w * self.h, np.int32)
+        out = np.zeros(sum(a * b for a, b in self.views) if self.views else self.w * self.h, np.int32)
         if lib().oracle_frame_pass_words(self.r, i, out.ctypes.data) != 0:
             raise IndexError(i)
         return out

@@ -373,10 +373,12 @@ inline uint32_t AsUint(float f) { uint32_t r; std::memcpy(&r, &f, 4); return r; 
 inline float AsFloat(uint32_t u) { float r; std::memcpy(&r, &u, 4); return r; }
 
 // raycast.cl:33-256 (ESVO descent in [1,2]^3 with block-cache faults)
-// Two guards make the reference's undefined reads explicit (both unreachable
-// on a well-formed cache): a pop that lands past the root ends the loop before
-// reading stack[scale >= 23], and a node or far index outside the cache ends
-// the ray with the iteration-limit error.
+// Three guards make the reference's undefined accesses explicit (all
+// unreachable on a well-formed cache and a tree of at most 23 levels): a pop
+// that lands past the root ends the loop before reading stack[scale >= 23]; a
+// node or far index outside the cache ends the ray with the iteration-limit
+// error; a node at scale 0 ends the ray like a leaf (its children would lie
+// below float resolution, and the reference would index its stack at -1).
 void Cast(const uint32_t* links, const uint32_t* far, int root, V4 p, V4 d, float coef, float bias, CastResult* r,
           uint32_t node_limit, uint32_t far_limit) {
   p.x = p.x + 1; p.y = p.y + 1; p.z = p.z + 1;
@@ -436,7 +438,7 @@ void Cast(const uint32_t* links, const uint32_t* far, int root, V4 p, V4 d, floa
       if (ofs >= node_limit) { r->error = 1; r->t = t_min; r->node = (int)parent; r->iterations = iter; return; }
       desc = links[ofs];
       ++r->fetches;
-      if (!(desc & 255) || tc_max * coef + bias >= scale_exp2) {
+      if (!(desc & 255) || scale == 0 || tc_max * coef + bias >= scale_exp2) {
         r->t = t_min; r->node = (int)ofs; r->dup = (int)((desc >> 9) & 1); r->iterations = iter;
         return;
       }
@@ -666,9 +668,17 @@ struct Feedback {
   }
 };
 
+// Views: the reference renders one (w, h) view per frame.  Several views of
+// one frame (the batched form, which has no reference counterpart) are traced
+// pass by pass together: their words are concatenated in view order, so the
+// feedback of a pass is one unique array over all views and NO_HIT is present
+// unless every ray of every view produced a word.
 struct Renderer {
   Cache* cache;
-  int w, h;
+  int w, h;                        // the first view
+  std::vector<int> vw, vh;
+  std::vector<size_t> voff;        // first pixel of each view
+  size_t total = 0;
   float lod = 1.5f;
   double time_limit = 1.0;
   int max_passes = 0;
@@ -701,7 +711,7 @@ struct Renderer {
     const uint8_t* col = Colors();
     long long fetches = 0, fars = 0, iters = 0, rays = 0, hits = 0;
 #pragma omp parallel for schedule(dynamic, 256) reduction(+ : fetches, fars, iters, rays, hits)
-    for (int i = 0; i < w * h; ++i) {
+    for (long long i = 0; i < (long long)total; ++i) {
       CastResult r{};
       bool live = !Done(st[i]);
       words[i] = TracePixel(st[i], *cache, links, nrm, col, &r);
@@ -716,15 +726,35 @@ struct Renderer {
   }
 
   // GPURayTracer::RenderFrame (gpu-ray-tracer.cpp:66-227)
+  void SetViews(int n, const int* ws, const int* hs) {
+    vw.assign(ws, ws + n);
+    vh.assign(hs, hs + n);
+    voff.clear();
+    total = 0;
+    for (int v = 0; v < n; ++v) {
+      voff.push_back(total);
+      total += (size_t)ws[v] * hs[v];
+    }
+    w = ws[0];
+    h = hs[0];
+  }
+
+  // InitTracingFrame for every view; m holds one matrix per view
+  void InitViews(const float* m) {
+    st.resize(total);
+    words.resize(total);
+    for (size_t v = 0; v < vw.size(); ++v)
+      for (int y = 0; y < vh[v]; ++y)
+        for (int x = 0; x < vw[v]; ++x)
+          InitRay(st[voff[v] + (size_t)y * vw[v] + x], x, y, vw[v], vh[v], m + 16 * v, lod);
+  }
+
   bool Frame(const float* m) {
     auto t0 = std::chrono::steady_clock::now();
-    st.resize((size_t)w * h);
-    words.resize((size_t)w * h);
-    uniq.resize((size_t)w * h);
-    image.resize((size_t)w * h * 4);
+    uniq.resize(total);
+    image.resize(total * 4);
     pass_words.clear();
-    for (int y = 0; y < h; ++y)
-      for (int x = 0; x < w; ++x) InitRay(st[(size_t)y * w + x], x, y, w, h, m, lod);
+    InitViews(m);
     cache->StartSession();
     bool ok = true;
     int it;
@@ -735,7 +765,7 @@ struct Renderer {
       if (it > 0 && el > time_limit) break;
       if (max_passes > 0 && it + 1 >= max_passes && it > 0) break;
       sorted = words;
-      int count = Unique(sorted.data(), w * h, cache->nib, uniq.data());
+      int count = Unique(sorted.data(), (int)total, cache->nib, uniq.data());
       fb.Decode(uniq.data(), count);
       cache->StartTransaction();
       for (int b : fb.hits) cache->MarkUsed(b);
@@ -753,7 +783,7 @@ struct Renderer {
     const int8_t* nrm = Normals();
     const uint8_t* col = Colors();
 #pragma omp parallel for schedule(static)
-    for (int i = 0; i < w * h; ++i) FinishPixel(st[i], nrm, col, &image[(size_t)i * 4]);
+    for (long long i = 0; i < (long long)total; ++i) FinishPixel(st[i], nrm, col, &image[(size_t)i * 4]);
     return ok;
   }
 };
@@ -813,8 +843,23 @@ void oracle_cache_counters(void* cp, long long* out3) {
 void* oracle_renderer_create(void* cache, int w, int h, float lod, double time_limit, int max_passes) {
   Renderer* r = new Renderer();
   r->cache = static_cast<Cache*>(cache);
-  r->w = w; r->h = h; r->lod = lod; r->time_limit = time_limit; r->max_passes = max_passes;
+  r->SetViews(1, &w, &h);
+  r->lod = lod; r->time_limit = time_limit; r->max_passes = max_passes;
   return r;
+}
+void* oracle_renderer_create_views(void* cache, int n, const int* ws, const int* hs, float lod, double time_limit,
+                                   int max_passes) {
+  Renderer* r = new Renderer();
+  r->cache = static_cast<Cache*>(cache);
+  r->SetViews(n, ws, hs);
+  r->lod = lod; r->time_limit = time_limit; r->max_passes = max_passes;
+  return r;
+}
+int oracle_frame_view_image(void* rp, int view, unsigned char* out) {
+  Renderer* r = static_cast<Renderer*>(rp);
+  if (view < 0 || view >= (int)r->vw.size()) return -1;
+  std::memcpy(out, r->image.data() + r->voff[view] * 4, (size_t)r->vw[view] * r->vh[view] * 4);
+  return 0;
 }
 void oracle_renderer_destroy(void* r) { delete static_cast<Renderer*>(r); }
 void oracle_renderer_record(void* r, int on) { static_cast<Renderer*>(r)->record = on != 0; }
@@ -844,16 +889,13 @@ void oracle_renderer_counters(void* rp, long long* out6) {
 // writes per-pixel words and RGBA (done pixels final, others unfinished).
 int oracle_trace_once(void* rp, const float* m, int* words_out, unsigned char* rgba_out) {
   Renderer* r = static_cast<Renderer*>(rp);
-  r->st.resize((size_t)r->w * r->h);
-  r->words.resize((size_t)r->w * r->h);
-  for (int y = 0; y < r->h; ++y)
-    for (int x = 0; x < r->w; ++x) InitRay(r->st[(size_t)y * r->w + x], x, y, r->w, r->h, m, r->lod);
+  r->InitViews(m);
   r->Pass();
   if (words_out) std::memcpy(words_out, r->words.data(), r->words.size() * 4);
   if (rgba_out) {
     const int8_t* nrm = r->Normals();
     const uint8_t* col = r->Colors();
-    for (int i = 0; i < r->w * r->h; ++i) {
+    for (long long i = 0; i < (long long)r->total; ++i) {
       RayState s = r->st[i];
       FinishPixel(s, nrm, col, rgba_out + (size_t)i * 4);
     }

@@ -127,6 +127,14 @@ def lib():
         "rayt_renderer_stats": (i32, [vp, C.POINTER(FrameStats)]),
         "rayt_renderer_count_fetches": (i32, [vp, C.POINTER(f32), C.POINTER(C.c_int64)]),
         "rayt_renderer_time_pass": (i32, [vp, C.POINTER(f32), i32, C.POINTER(f32)]),
+        "rayt_renderer_create_views": (i32, [vp, i32, C.POINTER(i32), C.POINTER(i32), C.POINTER(vp)]),
+        "rayt_render_views": (i32, [vp, C.POINTER(f32), i32]),
+        "rayt_renderer_view_count": (i32, [vp]),
+        "rayt_renderer_view_image": (i32, [vp, i32, C.POINTER(vp)]),
+        "rayt_renderer_read_view_image": (i32, [vp, i32, vp, C.c_size_t]),
+        "rayt_renderer_set_launch_shape": (i32, [vp, i32, i32, i32, i32]),
+        "rayt_renderer_get_launch_shape": (i32, [vp, C.POINTER(i32)]),
+        "rayt_renderer_autotune": (i32, [vp, C.POINTER(f32), i32, C.POINTER(i32)]),
         "rayt_sort_i32": (i32, [vp, i32, vp]),
         "rayt_scan_i32": (i32, [vp, i32, vp]),
         "rayt_feedback_unique": (i32, [vp, i32, i32, vp, C.POINTER(i32), vp]),
@@ -147,6 +155,11 @@ def _check(rc):
 
 def _mat(view_proj_inv):
     m = np.ascontiguousarray(np.asarray(view_proj_inv, dtype=np.float32).reshape(16))
+    return m, m.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _mats(view_proj_invs, n):
+    m = np.ascontiguousarray(np.asarray(view_proj_invs, dtype=np.float32).reshape(n * 16))
     return m, m.ctypes.data_as(C.POINTER(C.c_float))
 
 
@@ -309,12 +322,34 @@ class GPUOctreeCacheManager:
 
 
 class GPURayTracer:
-    def __init__(self, cache_manager, frame_width, frame_height):
+    """GPURayTracer (rayt/GPU_renderer/gpu-ray-tracer.h:11-55).
+
+    GPURayTracer(cache, w, h) is the reference's one-view renderer.
+    GPURayTracer.views(cache, [(w, h), ...]) is the batched form: every frame
+    (RenderViews) traces all views in the same launches and cache session."""
+
+    def __init__(self, cache_manager, frame_width, frame_height, _sizes=None):
         self.cache = cache_manager
-        self.width, self.height = frame_width, frame_height
         h = C.c_void_p()
-        _check(lib().rayt_renderer_create(cache_manager.handle, frame_width, frame_height, C.byref(h)))
+        if _sizes is None:
+            self.sizes = [(frame_width, frame_height)]
+            _check(lib().rayt_renderer_create(cache_manager.handle, frame_width, frame_height, C.byref(h)))
+        else:
+            self.sizes = [(int(w), int(hh)) for w, hh in _sizes]
+            n = len(self.sizes)
+            ws = (C.c_int * n)(*[w for w, _ in self.sizes])
+            hs = (C.c_int * n)(*[hh for _, hh in self.sizes])
+            _check(lib().rayt_renderer_create_views(cache_manager.handle, n, ws, hs, C.byref(h)))
+        self.width, self.height = self.sizes[0]
         self._h = h
+
+    @classmethod
+    def views(cls, cache_manager, sizes):
+        return cls(cache_manager, 0, 0, _sizes=list(sizes))
+
+    @property
+    def n_views(self):
+        return len(self.sizes)
 
     def set_frame_time_limit(self, seconds):
         _check(lib().rayt_renderer_set_frame_time_limit(self._h, seconds))
@@ -337,25 +372,48 @@ class GPURayTracer:
         m, p = _mat(camera_or_matrix)
         _check(lib().rayt_render_frame(self._h, p))
 
+    def RenderViews(self, matrices):
+        """One frame of every view; matrices: n_views view_proj_inv matrices."""
+        mats = [c.view_proj_inv() if isinstance(c, Camera) else c for c in matrices]
+        m, p = _mats(mats, self.n_views)
+        _check(lib().rayt_render_views(self._h, p, self.n_views))
+
+    def set_launch_shape(self, tile_w_log2, refill, ctas_per_sm=0, step_budget=16):
+        """See rayt_renderer_set_launch_shape; results do not depend on it."""
+        _check(lib().rayt_renderer_set_launch_shape(self._h, tile_w_log2, refill, ctas_per_sm, step_budget))
+
+    def launch_shape(self):
+        """(tile_w_log2, refill, ctas_per_sm, step_budget)"""
+        out = (C.c_int * 4)()
+        _check(lib().rayt_renderer_get_launch_shape(self._h, out))
+        return tuple(out[:])
+
+    def autotune(self, matrices, reps=3):
+        m, p = _mats(matrices, self.n_views)
+        out = (C.c_int * 4)()
+        _check(lib().rayt_renderer_autotune(self._h, p, reps, out))
+        return tuple(out[:])
+
     def stream_handle(self):
         """The cudaStream_t (as an int) the renderer runs on."""
         p = C.c_void_p()
         _check(lib().rayt_renderer_stream(self._h, C.byref(p)))
         return p.value or 0
 
-    def out_image_device_ptr(self):
+    def out_image_device_ptr(self, view=0):
         p = C.c_void_p()
-        _check(lib().rayt_renderer_image(self._h, C.byref(p)))
+        _check(lib().rayt_renderer_view_image(self._h, view, C.byref(p)))
         return p.value
 
-    def read_image(self, out=None):
+    def read_image(self, out=None, view=0):
+        w, h = self.sizes[view]
         if out is None:
-            out = np.zeros((self.height, self.width, 4), np.uint8)
-        _check(lib().rayt_renderer_read_image(self._h, out.ctypes.data, out.nbytes))
+            out = np.zeros((h, w, 4), np.uint8)
+        _check(lib().rayt_renderer_read_view_image(self._h, view, out.ctypes.data, out.nbytes))
         return out
 
     def pass_words(self, p):
-        out = np.zeros(self.width * self.height, np.int32)
+        out = np.zeros(sum(w * h for w, h in self.sizes), np.int32)
         _check(lib().rayt_renderer_pass_words(self._h, p, out.ctypes.data, out.size))
         return out
 
@@ -365,13 +423,13 @@ class GPURayTracer:
         return {k: getattr(s, k) for k, _ in FrameStats._fields_}
 
     def count_fetches(self, view_proj_inv):
-        m, p = _mat(view_proj_inv)
+        m, p = _mats(view_proj_inv, self.n_views)
         out = (C.c_int64 * 6)()
         _check(lib().rayt_renderer_count_fetches(self._h, p, out))
         return dict(zip(["rays", "link_fetches", "far_fetches", "iterations", "hits", "faults"], out[:]))
 
     def time_pass(self, view_proj_inv, reps):
-        m, p = _mat(view_proj_inv)
+        m, p = _mats(view_proj_inv, self.n_views)
         ms = C.c_float()
         _check(lib().rayt_renderer_time_pass(self._h, p, reps, C.byref(ms)))
         return ms.value

@@ -22,43 +22,73 @@ constexpr int32_t kNoHit = 0x7fffffff;
 constexpr uint32_t kRootParent = (1u << 24) - 1;
 
 // ---- traversal ----------------------------------------------------------------
+// Views' images (and recorded feedback words) share one buffer; view v starts
+// at pixel pix_base (a multiple of 64).  A ray is identified by its pixel's
+// index in that buffer, below 2^30.
+constexpr int kMaxViews = 512;
+constexpr int kViewsPerLaunch = 64;   // view descriptors travel in the launch parameters
+
+// One view of a tracing launch.
+struct ViewDesc {
+  float m[16];             // view_proj_inv, row-major
+  int width, height;
+  int tiles_x;             // columns of 32-pixel tiles
+  int tile_base;           // first tile of this view in the launch's tile space
+  float lod;               // lod_voxel_size
+  int pix_base;            // first pixel of the view in the shared image buffer
+};
+
 struct TraceParams {
   // cache (the reference's cache format)
   const uint32_t* links;
   const uint32_t* far_ptrs;
-  const char4* normals;   // may be null
-  const uchar4* colors;   // may be null
+  const char4* normals;    // may be null
+  const uchar4* colors;    // may be null
   int root;
   int nodes_in_block;
-  uint32_t node_limit;    // nodes in the cache (max_blocks * nodes_in_block)
-  uint32_t far_limit;     // far pointers in the cache (max_blocks * 8)
-  // frame
-  int width, height;
-  float m[16];            // view_proj_inv, row-major
-  float lod;              // lod_voxel_size
-  float bg[4];            // background colour (0, 216/255, 1, 1)
-  // ray state of faulted rays, indexed by pixel
-  float4* origin;         // xyz origin, w LOD bias
-  float4* dir;            // xyz direction, w LOD coefficient
-  int* fault_parent;
-  // active lists (rays to trace this pass, rays that faulted)
-  const int* active_in;
-  const int* n_active_in;
-  int* active_out;
-  int* n_active_out;
-  // outputs
-  uchar4* image;
-  int* words_dense;       // optional per-pixel feedback words (debug/parity)
-  uint32_t* fault_bits;   // one bit per tree block
-  int fault_bit_limit;    // number of tree blocks (bits in fault_bits)
-  uint32_t* hit_bits;     // bit 2*cache_block + dup
-  int* n_words;           // number of non-NO_HIT words this pass
+  uint32_t node_limit;     // nodes in the cache (max_blocks * nodes_in_block)
+  uint32_t far_limit;      // far pointers in the cache (max_blocks * 8)
+  float bg[4];             // background colour (0, 216/255, 1, 1)
+  // outputs of every view
+  uchar4* image;           // RGBA8, row 0 of each view at the bottom
+  int32_t* words_dense;    // optional per-pixel feedback words (recording)
+  // first pass: the views of this launch and their tiles (32 rays each)
+  int n_views;
+  int total_tiles;
+  int tile_w_log2;         // a warp's 32 first-pass rays cover (1 << tile_w_log2) x (32 >> tile_w_log2) pixels
+  // faulted rays carried between passes: record i of the input list, and the
+  // output list the rays that fault in this pass are appended to
+  const float4* in_origin;
+  const float4* in_dir;
+  const int* in_parent;
+  const uint32_t* in_ray;
+  const int* n_in;
+  float4* out_origin;      // xyz origin, w LOD bias
+  float4* out_dir;         // xyz direction, w LOD coefficient
+  int* out_parent;
+  uint32_t* out_ray;
+  int* n_out;
+  // feedback
+  uint32_t* fault_bits;    // one bit per tree block
+  int fault_bit_limit;     // number of tree blocks (bits in fault_bits)
+  uint32_t* hit_bits;      // bit 2*cache_block + dup
+  int* n_words;            // number of non-NO_HIT words this pass
   unsigned long long* counters;  // optional: rays, link fetches, far fetches, iterations, hits, faults
+  // persistent kernel only
+  int* work;               // work counter, zero before the launch
+  int refill;              // idle lanes that let a warp take new rays (< 32)
+  int step_budget;         // iterations a warp runs between refill checks
+  ViewDesc views[kViewsPerLaunch];
 };
 
-// first: rays come from the camera (every pixel); otherwise from active_in.
-cudaError_t launch_trace(const TraceParams& p, bool first, bool count, int max_active, cudaStream_t s);
-cudaError_t launch_finish(const TraceParams& p, int max_active, cudaStream_t s);
+// first: rays come from the views' cameras; otherwise from the input list.
+// refill = 32: one thread per ray over `rays` threads (rays = total_tiles * 32
+// on the first pass, an upper bound of *n_in after it); refill < 32: the
+// persistent work-stealing kernel over `grid` CTAs.
+cudaError_t launch_trace(const TraceParams& p, bool first, bool count, int rays, int grid, cudaStream_t s);
+// Resident CTAs of the persistent traversal kernel on the current device.
+int trace_persistent_grid(bool first, bool count);
+cudaError_t launch_finish(const TraceParams& p, int max_rays, cudaStream_t s);
 cudaError_t launch_fill_i32(int* p, int32_t v, size_t n, cudaStream_t s);
 
 // Feedback bitmaps -> the reference's sorted unique array.
@@ -70,7 +100,8 @@ struct UniqueFromBitsParams {
   const int* n_words;
   int total_pixels;
   int32_t* unique_out;   // room for fault bits + hit bits + 1
-  int* counts_out;       // [0] unique count (incl. NO_HIT), [1] fault count
+  const int* n_rays;     // rays the pass appended to its output list
+  int* counts_out;       // [0] unique count (incl. NO_HIT), [1] fault count, [2] *n_rays
 };
 cudaError_t launch_unique_from_bits(const UniqueFromBitsParams& p, cudaStream_t s);
 

@@ -2,15 +2,20 @@
 // (rayt/GPU_renderer/gpu-ray-tracer.cpp:66-227) and the host half of its
 // RayTracingFeedbackExtractor (rayt/GPU_renderer/ray-tracing-feedback-extractor.cpp:100-185).
 //
-// Per pass: one traversal launch (first pass: every pixel from the camera,
-// later passes: only rays that faulted), one launch that turns the feedback
-// bitmaps into the reference's sorted unique array (written straight into
-// host-mapped pinned memory), one stream synchronisation, then the host runs
-// the reference's decode (all faults, plus a window of at most 4000 hits that
+// A renderer holds one view (the reference's GPURayTracer) or several views of
+// any sizes that share one cache session per frame (batched form).  Per pass:
+// one traversal launch over all views (first pass: every pixel from its
+// view's camera, later passes: only rays that faulted; more than 64 views take
+// one first-pass launch per 64), one launch that turns the feedback bitmaps
+// into the reference's sorted unique array (written straight into host-mapped
+// pinned memory), one stream synchronisation, then the host runs the
+// reference's decode (all faults, plus a window of at most 4000 hits that
 // starts at rand() % hits) and its cache transaction.  Block uploads go onto
 // the same stream, so the next pass sees them without another wait.  The loop
 // ends exactly where the reference's does: no faults, cache filled during the
 // session, or (after the second pass) the time limit / pass cap.
+#include <algorithm>
+#include <climits>
 #include <chrono>
 #include <cstring>
 #include <memory>
@@ -20,14 +25,23 @@
 
 namespace rayt {
 
+// Faulted-ray records carried from one pass to the next.
+struct RayList {
+  float4* origin = nullptr;  // xyz advanced to the fault, w LOD bias
+  float4* dir = nullptr;     // xyz direction, w LOD coefficient
+  int* parent = nullptr;     // node the ray faulted under
+  uint32_t* ray = nullptr;   // view << kRayPixelBits | pixel
+};
+
 class Renderer {
  public:
   ~Renderer();
-  int Init(Cache* cache, int w, int h);
+  int Init(Cache* cache, int n_views, const int* widths, const int* heights);
   int Frame(const float* m);
   int CountFetches(const float* m, int64_t* counts);
   int TimePass(const float* m, int reps, float* ms);
-  int ReadImage(void* host, size_t bytes);
+  int Autotune(const float* m, int reps, int* best);
+  int ReadImage(int view, void* host, size_t bytes);
   int PassWords(int pass, int32_t* host, size_t count) const;
 
   double time_limit = 1.0;  // the reference's default (gpu-ray-tracer.cpp:30-31)
@@ -36,29 +50,37 @@ class Renderer {
   bool record = false;
   LibcRand rand;
   rayt_frame_stats stats{};
-  uchar4* image() const { return d_image_; }
+  // traversal launch shape
+  int tile_w_log2 = 2;   // 4x8 pixel tiles (fastest on the 1080p flythrough)
+  int refill = 32;       // 32: one thread per ray; below: the persistent kernel (slower on every
+                         // measured frame, kept for the autotuner)
+  int ctas_per_sm = 0;   // persistent kernel: 0 = as many as fit
+  int step_budget = 16;  // persistent kernel: iterations between refill checks
+  int n_views() const { return (int)views_.size(); }
+  uchar4* image(int v) const { return d_images_ + views_[v].pix_base; }
   cudaStream_t stream() const { return s_; }
 
  private:
+  static constexpr int kBlockInts = 16;  // pass block: {words, rays out, pad, pad, work counter per launch group}
   Cache* cache_ = nullptr;
-  int w_ = 0, h_ = 0;
+  int total_pixels_ = 0, padded_pixels_ = 0;
   int expected_faults_ = 1 << 16;  // ray-tracing-feedback-extractor.cpp:22-23
   int hits_to_extract_ = 4000;
   cudaStream_t s_ = nullptr;
-  uchar4* d_image_ = nullptr;
-  float4* d_origin_ = nullptr;
-  float4* d_dir_ = nullptr;
-  int* d_parent_ = nullptr;
-  int* d_active_[2] = {nullptr, nullptr};
-  int* d_dense_ = nullptr;
-  uint32_t* d_bits_ = nullptr;
+  std::vector<ViewDesc> views_;     // sizes, tile layout and matrices of the current frame
+  std::vector<int> group_tiles_;    // first-pass tiles per launch group of kViewsPerLaunch views
+  uchar4* d_images_ = nullptr;      // every view's image at its pix_base
+  int32_t* d_dense_ = nullptr;      // recorded feedback words, same layout
+  RayList lists_[2];
+  // [pass block 0][fault bits][hit bits][pass block 1]: pass k clears its own
+  // block and the bitmaps with one memset and reads the other block's ray
+  // count as its input.
+  int* d_state_ = nullptr;
   int fault_words_ = 0, hit_words_ = 0;
-  int* d_counters_ = nullptr;        // [0] words, [1],[2] active counts of the two lists
-  int* h_pass_ = nullptr;            // pinned copy of d_counters_
   unsigned long long* d_fetch_ = nullptr;
   int32_t* h_unique_ = nullptr;      // mapped pinned
   int32_t* d_unique_ = nullptr;
-  int* h_counts_ = nullptr;          // mapped pinned: unique count, fault count
+  int* h_counts_ = nullptr;          // mapped pinned: unique count, fault count, rays faulted
   int* d_counts_ = nullptr;
   int32_t* h_dense_ = nullptr;       // pinned, for recording
   uint8_t* d_flush_ = nullptr;       // L2 flush buffer for TimePass
@@ -66,25 +88,29 @@ class Renderer {
   std::vector<std::vector<int32_t>> pass_words_;
   std::vector<int> faults_, hits_, dup_hits_;
 
-  TraceParams Params(const float* m) const;
+  int* block(int k) const { return k ? d_state_ + kBlockInts + fault_words_ + hit_words_ : d_state_; }
+  int SetViews(const float* m);
+  TraceParams Params(int it) const;
+  int Grid(bool first, bool count) const;
   void Decode(int count);
   int Prepare(int it);
+  int Trace(int it, bool count, int rays);
+  int groups() const { return (int)group_tiles_.size(); }
 };
 
 Renderer::~Renderer() {
   if (s_) cudaStreamSynchronize(s_);
-  cudaFree(d_image_);
-  cudaFree(d_origin_);
-  cudaFree(d_dir_);
-  cudaFree(d_parent_);
-  cudaFree(d_active_[0]);
-  cudaFree(d_active_[1]);
+  cudaFree(d_images_);
+  for (auto& l : lists_) {
+    cudaFree(l.origin);
+    cudaFree(l.dir);
+    cudaFree(l.parent);
+    cudaFree(l.ray);
+  }
   cudaFree(d_dense_);
-  cudaFree(d_bits_);
-  cudaFree(d_counters_);
+  cudaFree(d_state_);
   cudaFree(d_fetch_);
   cudaFree(d_flush_);
-  cudaFreeHost(h_pass_);
   cudaFreeHost(h_unique_);
   cudaFreeHost(h_counts_);
   cudaFreeHost(h_dense_);
@@ -92,38 +118,80 @@ Renderer::~Renderer() {
     if (e) cudaEventDestroy(e);
 }
 
-int Renderer::Init(Cache* cache, int w, int h) {
-  if (w <= 0 || h <= 0 || (int64_t)w * h >= (1ll << 30)) return fail(RAYT_E_ARG, "frame size out of range");
+int Renderer::Init(Cache* cache, int n_views, const int* widths, const int* heights) {
+  if (n_views < 1 || n_views > kMaxViews) return fail(RAYT_E_ARG, "view count out of range (1..512)");
   cache_ = cache;
-  w_ = w;
-  h_ = h;
   s_ = cache->stream();
-  const size_t n = (size_t)w * h;
-  if (cudaMalloc(&d_image_, n * 4) != cudaSuccess || cudaMalloc(&d_origin_, n * 16) != cudaSuccess ||
-      cudaMalloc(&d_dir_, n * 16) != cudaSuccess || cudaMalloc(&d_parent_, n * 4) != cudaSuccess ||
-      cudaMalloc(&d_active_[0], n * 4) != cudaSuccess || cudaMalloc(&d_active_[1], n * 4) != cudaSuccess ||
-      cudaMalloc(&d_dense_, n * 4) != cudaSuccess || cudaMalloc(&d_counters_, 16 * 4) != cudaSuccess ||
+  views_.assign(n_views, ViewDesc{});
+  int64_t pixels = 0, padded = 0;
+  for (int v = 0; v < n_views; ++v) {
+    const int w = widths[v], h = heights[v];
+    if (w <= 0 || h <= 0 || (int64_t)w * h > (1 << 28)) return fail(RAYT_E_ARG, "view size out of range (at most 2^28 pixels)");
+    views_[v].width = w;
+    views_[v].height = h;
+    views_[v].pix_base = (int)padded;
+    pixels += (int64_t)w * h;
+    padded += ((int64_t)w * h + 63) & ~(int64_t)63;
+    if (padded >= (1 << 30)) return fail(RAYT_E_ARG, "total pixels of all views out of range (2^30)");
+  }
+  total_pixels_ = (int)pixels;
+  padded_pixels_ = (int)padded;
+  group_tiles_.assign((n_views + kViewsPerLaunch - 1) / kViewsPerLaunch, 0);
+  const size_t n = pixels;
+  if (cudaMalloc(&d_images_, (size_t)padded * 4) != cudaSuccess || cudaMalloc(&d_dense_, (size_t)padded * 4) != cudaSuccess ||
       cudaMalloc(&d_fetch_, 8 * 8) != cudaSuccess)
     return fail(RAYT_E_OOM, "renderer device allocation failed");
+  for (auto& l : lists_)
+    if (cudaMalloc(&l.origin, n * 16) != cudaSuccess || cudaMalloc(&l.dir, n * 16) != cudaSuccess ||
+        cudaMalloc(&l.parent, n * 4) != cudaSuccess || cudaMalloc(&l.ray, n * 4) != cudaSuccess)
+      return fail(RAYT_E_OOM, "ray list allocation failed");
   // one bit per block of the file; one bit per (cache block, duplicate flag)
   fault_words_ = (int)((cache->tree_blocks() + 31) / 32);
   hit_words_ = (int)(((uint64_t)cache->max_blocks() * 2 + 31) / 32);
   const size_t bit_words = (size_t)fault_words_ + hit_words_;
-  if (cudaMalloc(&d_bits_, bit_words * 4) != cudaSuccess) return fail(RAYT_E_OOM, "feedback bitmap allocation failed");
+  if (cudaMalloc(&d_state_, (bit_words + 2 * kBlockInts) * 4) != cudaSuccess)
+    return fail(RAYT_E_OOM, "feedback bitmap allocation failed");
   if (cudaHostAlloc(&h_unique_, (bit_words * 32 + 1) * 4, cudaHostAllocMapped) != cudaSuccess ||
-      cudaHostAlloc(&h_counts_, 4 * 4, cudaHostAllocMapped) != cudaSuccess ||
-      cudaHostAlloc(&h_pass_, 16 * 4, cudaHostAllocDefault) != cudaSuccess)
+      cudaHostAlloc(&h_counts_, 4 * 4, cudaHostAllocMapped) != cudaSuccess)
     return fail(RAYT_E_OOM, "pinned host allocation failed");
   RAYT_CUDA_TRY(cudaHostGetDevicePointer((void**)&d_unique_, h_unique_, 0));
   RAYT_CUDA_TRY(cudaHostGetDevicePointer((void**)&d_counts_, h_counts_, 0));
   for (auto& e : ev_) RAYT_CUDA_TRY(cudaEventCreate(&e));
-  RAYT_CUDA_TRY(cudaMemsetAsync(d_image_, 0, n * 4, s_));
+  RAYT_CUDA_TRY(cudaMemsetAsync(d_images_, 0, (size_t)padded * 4, s_));
+  RAYT_CUDA_TRY(cudaMemsetAsync(d_state_, 0, (bit_words + 2 * kBlockInts) * 4, s_));
   RAYT_CUDA_TRY(cudaStreamSynchronize(s_));
   return RAYT_OK;
 }
 
-TraceParams Renderer::Params(const float* m) const {
-  TraceParams p{};
+// Per-frame view descriptors: matrices, LOD and the tile layout of each
+// launch group (they travel in the launch parameters).
+int Renderer::SetViews(const float* m) {
+  if (tile_w_log2 < 0 || tile_w_log2 > 5) return fail(RAYT_E_ARG, "tile width out of range");
+  const int tw = 1 << tile_w_log2, th = 32 >> tile_w_log2;
+  for (int g = 0; g < groups(); ++g) {
+    int64_t tiles = 0;
+    const int end = std::min(n_views(), (g + 1) * kViewsPerLaunch);
+    for (int v = g * kViewsPerLaunch; v < end; ++v) {
+      ViewDesc& d = views_[v];
+      std::memcpy(d.m, m + 16 * v, sizeof(d.m));
+      d.lod = lod;
+      d.tiles_x = (d.width + tw - 1) / tw;
+      d.tile_base = (int)std::min<int64_t>(tiles, INT32_MAX);
+      tiles += (int64_t)d.tiles_x * ((d.height + th - 1) / th);
+    }
+    // the kernel counts first-pass rays (32 per tile) in int, with room for a
+    // counter to run past the end by one grab per warp
+    if (tiles * 32 > (int64_t)INT32_MAX - (1 << 24))
+      return fail(RAYT_E_ARG, "too many pixel tiles for this tile shape; use a tile shape closer to the views' aspect");
+    group_tiles_[g] = (int)tiles;
+  }
+  return RAYT_OK;
+}
+
+TraceParams Renderer::Params(int it) const {
+  const int k = it & 1;
+  TraceParams p;
+  std::memset(&p, 0, sizeof(p));
   p.links = cache_->links();
   p.far_ptrs = cache_->far_ptrs();
   p.normals = static_cast<const char4*>(cache_->channel("normals", 4));
@@ -132,23 +200,42 @@ TraceParams Renderer::Params(const float* m) const {
   p.nodes_in_block = cache_->nodes_in_block();
   p.node_limit = (uint32_t)cache_->max_blocks() * (uint32_t)cache_->nodes_in_block();
   p.far_limit = (uint32_t)cache_->max_blocks() * 8u;
-  p.width = w_;
-  p.height = h_;
-  std::memcpy(p.m, m, sizeof(p.m));
-  p.lod = lod;
   p.bg[0] = 0.0f;
   p.bg[1] = (float)(216 / 255.);  // the reference's background (gpu-ray-tracer.cpp:190)
   p.bg[2] = 1.0f;
   p.bg[3] = 1.0f;
-  p.origin = d_origin_;
-  p.dir = d_dir_;
-  p.fault_parent = d_parent_;
-  p.image = d_image_;
-  p.fault_bits = d_bits_;
+  p.image = d_images_;
+  p.words_dense = record ? d_dense_ : nullptr;
+  p.tile_w_log2 = tile_w_log2;
+  const RayList& in = lists_[1 - k];
+  const RayList& out = lists_[k];
+  p.in_origin = in.origin;
+  p.in_dir = in.dir;
+  p.in_parent = in.parent;
+  p.in_ray = in.ray;
+  p.n_in = block(1 - k) + 1;
+  p.out_origin = out.origin;
+  p.out_dir = out.dir;
+  p.out_parent = out.parent;
+  p.out_ray = out.ray;
+  p.n_out = block(k) + 1;
+  p.fault_bits = reinterpret_cast<uint32_t*>(d_state_ + kBlockInts);
   p.fault_bit_limit = (int)cache_->tree_blocks();
-  p.hit_bits = d_bits_ + fault_words_;
-  p.n_words = d_counters_;
+  p.hit_bits = reinterpret_cast<uint32_t*>(d_state_ + kBlockInts + fault_words_);
+  p.n_words = block(k);
+  p.work = block(k) + 4;
+  p.refill = refill;
+  p.step_budget = step_budget;
   return p;
+}
+
+int Renderer::Grid(bool first, bool count) const {
+  const int full = trace_persistent_grid(first, count);
+  if (ctas_per_sm <= 0) return full;
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return std::min(full, sms * ctas_per_sm);
 }
 
 // ProcessUnique + AdjustExpectedFaults (ray-tracing-feedback-extractor.cpp:108-185)
@@ -194,13 +281,32 @@ void Renderer::Decode(int count) {
   else if ((int)faults_.size() > expected_faults_) expected_faults_ *= 2;
 }
 
-
-// Clears the per-pass feedback state; pass `it` appends faulted rays to list it % 2.
+// Clears pass `it`'s block and the feedback bitmaps (one contiguous range).
 int Renderer::Prepare(int it) {
-  RAYT_CUDA_TRY(cudaMemsetAsync(d_bits_, 0, ((size_t)fault_words_ + hit_words_) * 4, s_));
-  RAYT_CUDA_TRY(cudaMemsetAsync(d_counters_, 0, 4, s_));
-  RAYT_CUDA_TRY(cudaMemsetAsync(d_counters_ + 1 + (it & 1), 0, 4, s_));
-  if (record) RAYT_CUDA_TRY(launch_fill_i32(d_dense_, kNoHit, (size_t)w_ * h_, s_));
+  const size_t words = kBlockInts + (size_t)fault_words_ + hit_words_;
+  RAYT_CUDA_TRY(cudaMemsetAsync((it & 1) ? d_state_ + kBlockInts : d_state_, 0, words * 4, s_));
+  if (record) RAYT_CUDA_TRY(launch_fill_i32(d_dense_, kNoHit, (size_t)padded_pixels_, s_));
+  return RAYT_OK;
+}
+
+// Pass `it`: the first pass launches once per group of kViewsPerLaunch views;
+// later passes once over the `rays` faulted rays of the previous pass.
+int Renderer::Trace(int it, bool count, int rays) {
+  TraceParams p = Params(it);
+  if (count) p.counters = d_fetch_;
+  const int grid = refill < 32 ? Grid(it == 0, count) : 0;
+  if (it > 0) {
+    RAYT_CUDA_TRY(launch_trace(p, false, count, rays, grid, s_));
+    return RAYT_OK;
+  }
+  for (int g = 0; g < groups(); ++g) {
+    const int first = g * kViewsPerLaunch, end = std::min(n_views(), first + kViewsPerLaunch);
+    p.n_views = end - first;
+    std::memcpy(p.views, views_.data() + first, (size_t)p.n_views * sizeof(ViewDesc));
+    p.total_tiles = group_tiles_[g];
+    p.work = block(0) + 4 + g;
+    RAYT_CUDA_TRY(launch_trace(p, true, count, group_tiles_[g] * 32, grid, s_));
+  }
   return RAYT_OK;
 }
 
@@ -213,40 +319,38 @@ int Renderer::Frame(const float* m) {
   const int64_t h2d0 = cache_->stats().bytes_h2d;
   int launches = 0;
   int64_t d2h = 0;
-  int rc = cache_->StartSession();
+  int rc = SetViews(m);
   if (rc != RAYT_OK) return rc;
-  const int total = w_ * h_;
+  rc = cache_->StartSession();
+  if (rc != RAYT_OK) return rc;
+  const int total = total_pixels_;
   int active_prev = total;  // rays traced by the first pass
   float ms_trace = 0, ms_fb = 0, ms_up = 0;
   int it;
   for (it = 0;; ++it) {
     if ((rc = Prepare(it)) != RAYT_OK) break;
-    TraceParams p = Params(m);
-    p.active_in = d_active_[(it + 1) & 1];
-    p.n_active_in = d_counters_ + 1 + ((it + 1) & 1);
-    p.active_out = d_active_[it & 1];
-    p.n_active_out = d_counters_ + 1 + (it & 1);
-    p.words_dense = record ? d_dense_ : nullptr;
     RAYT_CUDA_TRY(cudaEventRecord(ev_[0], s_));
-    RAYT_CUDA_TRY(launch_trace(p, it == 0, false, active_prev, s_));
-    launches += (it == 0 || active_prev > 0) ? 1 : 0;
+    if (it == 0 || active_prev > 0) {
+      if ((rc = Trace(it, false, active_prev)) != RAYT_OK) break;
+      launches += it == 0 ? groups() : 1;
+    }
     RAYT_CUDA_TRY(cudaEventRecord(ev_[1], s_));
     UniqueFromBitsParams q{};
-    q.fault_bits = d_bits_;
+    q.fault_bits = reinterpret_cast<const uint32_t*>(d_state_ + kBlockInts);
     q.fault_words = fault_words_;
-    q.hit_bits = d_bits_ + fault_words_;
+    q.hit_bits = reinterpret_cast<const uint32_t*>(d_state_ + kBlockInts + fault_words_);
     q.hit_words = hit_words_;
-    q.n_words = d_counters_;
+    q.n_words = block(it & 1);
+    q.n_rays = block(it & 1) + 1;
     q.total_pixels = total;
     q.unique_out = d_unique_;
     q.counts_out = d_counts_;
     RAYT_CUDA_TRY(launch_unique_from_bits(q, s_));
     launches += 1 + (record ? 1 : 0);
     RAYT_CUDA_TRY(cudaEventRecord(ev_[2], s_));
-    RAYT_CUDA_TRY(cudaMemcpyAsync(h_pass_, d_counters_, 3 * 4, cudaMemcpyDeviceToHost, s_));
     if (record) {
-      if (!h_dense_) RAYT_CUDA_TRY(cudaHostAlloc(&h_dense_, (size_t)total * 4, cudaHostAllocDefault));
-      RAYT_CUDA_TRY(cudaMemcpyAsync(h_dense_, d_dense_, (size_t)total * 4, cudaMemcpyDeviceToHost, s_));
+      if (!h_dense_) RAYT_CUDA_TRY(cudaHostAlloc(&h_dense_, (size_t)padded_pixels_ * 4, cudaHostAllocDefault));
+      RAYT_CUDA_TRY(cudaMemcpyAsync(h_dense_, d_dense_, (size_t)padded_pixels_ * 4, cudaMemcpyDeviceToHost, s_));
     }
     RAYT_CUDA_TRY(cudaStreamSynchronize(s_));
     float a = 0, b = 0;
@@ -255,9 +359,14 @@ int Renderer::Frame(const float* m) {
     ms_trace += a;
     ms_fb += b;
     stats.rays_traced += active_prev;
-    if (record) pass_words_.emplace_back(h_dense_, h_dense_ + total);
-    const int active_now = h_pass_[1 + (it & 1)];
-    d2h += 3 * 4 + 2 * 4 + (int64_t)h_counts_[0] * 4;  // counters, counts, unique array
+    if (record) {  // views in order, without the padding between them
+      pass_words_.emplace_back();
+      for (const ViewDesc& v : views_)
+        pass_words_.back().insert(pass_words_.back().end(), h_dense_ + v.pix_base,
+                                  h_dense_ + v.pix_base + (size_t)v.width * v.height);
+    }
+    const int active_now = h_counts_[2];
+    d2h += 3 * 4 + (int64_t)h_counts_[0] * 4;  // counts, unique array (mapped reads)
 
     // the reference always gives the frame one round of loading, then stops
     // on its wall-clock limit (gpu-ray-tracer.cpp:123-125)
@@ -289,10 +398,14 @@ int Renderer::Frame(const float* m) {
   if (rc != RAYT_OK) return rc;
   if (src != RAYT_OK) return src;
   // FinishTracingFrame for the rays still faulted, against the cache as it is now
-  TraceParams p = Params(m);
-  p.active_in = d_active_[it & 1];
-  p.n_active_in = d_counters_ + 1 + (it & 1);
-  RAYT_CUDA_TRY(launch_finish(p, active_prev, s_));
+  const TraceParams p = Params(it);
+  TraceParams f = p;
+  f.in_origin = p.out_origin;
+  f.in_dir = p.out_dir;
+  f.in_parent = p.out_parent;
+  f.in_ray = p.out_ray;
+  f.n_in = p.n_out;
+  RAYT_CUDA_TRY(launch_finish(f, active_prev, s_));
   if (active_prev > 0) ++launches;
   RAYT_CUDA_TRY(cudaStreamSynchronize(s_));
   if (stats.passes > 1 || stats.faults) {
@@ -311,14 +424,11 @@ int Renderer::Frame(const float* m) {
 }
 
 int Renderer::CountFetches(const float* m, int64_t* counts) {
-  int rc = Prepare(0);
+  int rc = SetViews(m);
+  if (rc == RAYT_OK) rc = Prepare(0);
   if (rc != RAYT_OK) return rc;
   RAYT_CUDA_TRY(cudaMemsetAsync(d_fetch_, 0, 8 * 8, s_));
-  TraceParams p = Params(m);
-  p.active_out = d_active_[0];
-  p.n_active_out = d_counters_ + 1;
-  p.counters = d_fetch_;
-  RAYT_CUDA_TRY(launch_trace(p, true, true, 0, s_));
+  if ((rc = Trace(0, true, 0)) != RAYT_OK) return rc;
   unsigned long long h[8];
   RAYT_CUDA_TRY(cudaMemcpyAsync(h, d_fetch_, sizeof(h), cudaMemcpyDeviceToHost, s_));
   RAYT_CUDA_TRY(cudaStreamSynchronize(s_));
@@ -331,16 +441,14 @@ int Renderer::CountFetches(const float* m, int64_t* counts) {
 int Renderer::TimePass(const float* m, int reps, float* ms) {
   const size_t flush = 256u << 20;
   if (!d_flush_ && cudaMalloc(&d_flush_, flush) != cudaSuccess) return fail(RAYT_E_OOM, "flush buffer allocation failed");
+  int rc = SetViews(m);
+  if (rc != RAYT_OK) return rc;
   float total = 0;
   for (int r = 0; r < reps; ++r) {
     RAYT_CUDA_TRY(cudaMemsetAsync(d_flush_, r & 255, flush, s_));
-    int rc = Prepare(0);
-    if (rc != RAYT_OK) return rc;
-    TraceParams p = Params(m);
-    p.active_out = d_active_[0];
-    p.n_active_out = d_counters_ + 1;
+    if ((rc = Prepare(0)) != RAYT_OK) return rc;
     RAYT_CUDA_TRY(cudaEventRecord(ev_[5], s_));
-    RAYT_CUDA_TRY(launch_trace(p, true, false, 0, s_));
+    if ((rc = Trace(0, false, 0)) != RAYT_OK) return rc;
     RAYT_CUDA_TRY(cudaEventRecord(ev_[6], s_));
     RAYT_CUDA_TRY(cudaEventSynchronize(ev_[6]));
     float a = 0;
@@ -351,9 +459,47 @@ int Renderer::TimePass(const float* m, int reps, float* ms) {
   return RAYT_OK;
 }
 
-int Renderer::ReadImage(void* host, size_t bytes) {
-  if (bytes < (size_t)w_ * h_ * 4) return fail(RAYT_E_ARG, "image buffer too small");
-  RAYT_CUDA_TRY(cudaMemcpyAsync(host, d_image_, (size_t)w_ * h_ * 4, cudaMemcpyDeviceToHost, s_));
+// Picks the traversal launch shape (tile shape, refill threshold and step
+// budget, CTAs per SM) with the shortest first pass over these views, timed
+// like TimePass.  The result is the renderer's shape from then on; best =
+// {tile_w_log2, refill, ctas_per_sm, step_budget}.
+int Renderer::Autotune(const float* m, int reps, int* best) {
+  struct Refill { int refill, budget; };
+  static const int kTiles[] = {2, 3, 4, 5};
+  static const Refill kRefill[] = {{32, 0}, {24, 16}, {16, 16}, {16, 32}, {8, 32}};
+  static const int kCtas[] = {0, 8, 6, 4};
+  const int save[4] = {tile_w_log2, refill, ctas_per_sm, step_budget};
+  float best_ms = 1e30f;
+  int b[4] = {save[0], save[1], save[2], save[3]};
+  for (int t : kTiles)
+    for (const Refill& r : kRefill)
+      for (int c : kCtas) {
+        tile_w_log2 = t;
+        refill = r.refill;
+        step_budget = r.budget;
+        ctas_per_sm = c;
+        float ms = 0;
+        int rc = TimePass(m, reps, &ms);
+        if (rc != RAYT_OK) {
+          tile_w_log2 = save[0], refill = save[1], ctas_per_sm = save[2], step_budget = save[3];
+          return rc;
+        }
+        if (ms < best_ms) best_ms = ms, b[0] = t, b[1] = r.refill, b[2] = c, b[3] = r.budget;
+      }
+  tile_w_log2 = b[0];
+  refill = b[1];
+  ctas_per_sm = b[2];
+  step_budget = b[3];
+  if (best)
+    for (int k = 0; k < 4; ++k) best[k] = b[k];
+  return RAYT_OK;
+}
+
+int Renderer::ReadImage(int view, void* host, size_t bytes) {
+  if (view < 0 || view >= n_views()) return fail(RAYT_E_ARG, "view index out of range");
+  const size_t n = (size_t)views_[view].width * views_[view].height * 4;
+  if (bytes < n) return fail(RAYT_E_ARG, "image buffer too small");
+  RAYT_CUDA_TRY(cudaMemcpyAsync(host, image(view), n, cudaMemcpyDeviceToHost, s_));
   RAYT_CUDA_TRY(cudaStreamSynchronize(s_));
   return RAYT_OK;
 }
@@ -377,7 +523,19 @@ extern "C" {
 int rayt_renderer_create(rayt_cache* cache, int width, int height, rayt_renderer** out) {
   if (!cache || !out) return fail(RAYT_E_ARG, "rayt_renderer_create: null argument");
   rayt::Renderer* r = new rayt::Renderer();
-  int rc = r->Init(reinterpret_cast<rayt::Cache*>(cache), width, height);
+  int rc = r->Init(reinterpret_cast<rayt::Cache*>(cache), 1, &width, &height);
+  if (rc != RAYT_OK) {
+    delete r;
+    return rc;
+  }
+  *out = reinterpret_cast<rayt_renderer*>(r);
+  return RAYT_OK;
+}
+int rayt_renderer_create_views(rayt_cache* cache, int n_views, const int* widths, const int* heights,
+                               rayt_renderer** out) {
+  if (!cache || !out || !widths || !heights) return fail(RAYT_E_ARG, "rayt_renderer_create_views: null argument");
+  rayt::Renderer* r = new rayt::Renderer();
+  int rc = r->Init(reinterpret_cast<rayt::Cache*>(cache), n_views, widths, heights);
   if (rc != RAYT_OK) {
     delete r;
     return rc;
@@ -413,7 +571,50 @@ int rayt_renderer_record_passes(rayt_renderer* r, int on) {
 }
 int rayt_render_frame(rayt_renderer* r, const float m[16]) {
   if (!r || !m) return fail(RAYT_E_ARG, "rayt_render_frame: null argument");
+  if (R(r)->n_views() != 1) return fail(RAYT_E_ARG, "rayt_render_frame: renderer has several views; use rayt_render_views");
   return R(r)->Frame(m);
+}
+int rayt_render_views(rayt_renderer* r, const float* m, int n_views) {
+  if (!r || !m) return fail(RAYT_E_ARG, "rayt_render_views: null argument");
+  if (n_views != R(r)->n_views()) return fail(RAYT_E_ARG, "rayt_render_views: matrix count differs from the renderer's views");
+  return R(r)->Frame(m);
+}
+int rayt_renderer_view_count(const rayt_renderer* r) {
+  if (!r) return fail(RAYT_E_ARG, "null renderer");
+  return reinterpret_cast<const rayt::Renderer*>(r)->n_views();
+}
+int rayt_renderer_view_image(rayt_renderer* r, int view, void** dev) {
+  if (!r || !dev) return fail(RAYT_E_ARG, "null argument");
+  if (view < 0 || view >= R(r)->n_views()) return fail(RAYT_E_ARG, "view index out of range");
+  *dev = R(r)->image(view);
+  return RAYT_OK;
+}
+int rayt_renderer_read_view_image(rayt_renderer* r, int view, void* host, size_t bytes) {
+  if (!r || !host) return fail(RAYT_E_ARG, "null argument");
+  return R(r)->ReadImage(view, host, bytes);
+}
+int rayt_renderer_set_launch_shape(rayt_renderer* r, int tile_w_log2, int refill, int ctas_per_sm, int step_budget) {
+  if (!r || tile_w_log2 < 0 || tile_w_log2 > 5 || refill < 1 || refill > 32 || ctas_per_sm < 0 ||
+      step_budget < 0 || (refill < 32 && step_budget < 1))
+    return fail(RAYT_E_ARG, "bad launch shape");
+  R(r)->tile_w_log2 = tile_w_log2;
+  R(r)->refill = refill;
+  R(r)->ctas_per_sm = ctas_per_sm;
+  R(r)->step_budget = step_budget;
+  return RAYT_OK;
+}
+int rayt_renderer_get_launch_shape(const rayt_renderer* r, int shape[4]) {
+  if (!r || !shape) return fail(RAYT_E_ARG, "null argument");
+  const rayt::Renderer* q = reinterpret_cast<const rayt::Renderer*>(r);
+  shape[0] = q->tile_w_log2;
+  shape[1] = q->refill;
+  shape[2] = q->ctas_per_sm;
+  shape[3] = q->step_budget;
+  return RAYT_OK;
+}
+int rayt_renderer_autotune(rayt_renderer* r, const float* m, int reps, int best[4]) {
+  if (!r || !m || reps < 1) return fail(RAYT_E_ARG, "bad argument");
+  return R(r)->Autotune(m, reps, best);
 }
 int rayt_renderer_stream(rayt_renderer* r, void** stream) {
   if (!r || !stream) return fail(RAYT_E_ARG, "null argument");
@@ -422,12 +623,12 @@ int rayt_renderer_stream(rayt_renderer* r, void** stream) {
 }
 int rayt_renderer_image(rayt_renderer* r, void** dev) {
   if (!r || !dev) return fail(RAYT_E_ARG, "null argument");
-  *dev = R(r)->image();
+  *dev = R(r)->image(0);
   return RAYT_OK;
 }
 int rayt_renderer_read_image(rayt_renderer* r, void* host, size_t bytes) {
   if (!r || !host) return fail(RAYT_E_ARG, "null argument");
-  return R(r)->ReadImage(host, bytes);
+  return R(r)->ReadImage(0, host, bytes);
 }
 int rayt_renderer_pass_words(rayt_renderer* r, int pass, int32_t* host, size_t count) {
   if (!r || !host) return fail(RAYT_E_ARG, "null argument");
@@ -438,11 +639,11 @@ int rayt_renderer_stats(const rayt_renderer* r, rayt_frame_stats* out) {
   *out = reinterpret_cast<const rayt::Renderer*>(r)->stats;
   return RAYT_OK;
 }
-int rayt_renderer_count_fetches(rayt_renderer* r, const float m[16], int64_t counts[6]) {
+int rayt_renderer_count_fetches(rayt_renderer* r, const float* m, int64_t counts[6]) {
   if (!r || !m || !counts) return fail(RAYT_E_ARG, "null argument");
   return R(r)->CountFetches(m, counts);
 }
-int rayt_renderer_time_pass(rayt_renderer* r, const float m[16], int reps, float* ms) {
+int rayt_renderer_time_pass(rayt_renderer* r, const float* m, int reps, float* ms) {
   if (!r || !m || !ms || reps < 1) return fail(RAYT_E_ARG, "bad argument");
   return R(r)->TimePass(m, reps, ms);
 }

@@ -1,4 +1,5 @@
-// Tracing pass, the hot path: one thread per primary ray.
+// Tracing pass, the hot path: a persistent, work-stealing traversal kernel
+// over the rays of one or many views.
 //
 // Per ray this fuses what the reference runs as separate full-frame kernels
 // with a 48-byte TracingState round trip through memory:
@@ -8,11 +9,17 @@
 //   shading         ProcessHit         (rayt/GPU_renderer/kernels/shading.cl:4-33)
 //   final colour    FinishTracingFrame (rayt/GPU_renderer/kernels/finish_tracing_frame.cl:3-24)
 //   block words     NodeToBlockKernel  (rayt/GPU_renderer/kernels/feedback_compression.cl:4-13)
-// A ray that finishes (hit, miss, iteration limit) writes its final RGBA8
-// pixel at once; only a ray that faults on a missing block stores its state
-// (advanced origin, direction, parent node) and joins the next pass's active
-// list, so later passes launch over faulted rays only.  Feedback goes straight
-// into two bitmaps (fault blocks, hit blocks) instead of a per-pixel word array.
+//
+// Scheduling: one CTA per SM slot stays resident; every warp takes rays from a
+// global counter (first pass: 32-pixel tiles of all views, 8x4 by default,
+// lane i of a tile = pixel (i % tile_w, i / tile_w); later passes: the
+// compacted list of rays that faulted).  A warp advances its rays one CastRay iteration at a time and,
+// as soon as `refill` lanes are idle, hands those lanes the next rays, so
+// lanes do not sit out a warp's longest ray and the grid has no tail.
+// A ray that ends (hit, miss, iteration limit) writes its final RGBA8 pixel;
+// a ray that faults on a missing block is appended with its state (advanced
+// origin, direction, parent node) to the next pass's list.  Feedback goes into
+// two bitmaps (fault blocks; hit cache blocks with the duplicate flag).
 //
 // FP32 arithmetic follows the reference's operation order exactly; the file is
 // compiled with --fmad=false and IEEE division/sqrt so no operation is fused or
@@ -25,16 +32,8 @@ namespace {
 constexpr int kSMax = 23;
 constexpr float kEps = 0.00000011920928955078125f;  // exp2(-S_MAX)
 constexpr int kIterLimit = 300;
-constexpr int kTileW = 8, kTileH = 4;  // one warp = 8x4 pixels
 constexpr int kBlockThreads = 128;
-
-struct Cast {
-  float t;
-  int node;
-  int fault_block;
-  int dup;
-  int error;
-};
+constexpr unsigned kFull = 0xffffffffu;
 
 __device__ __forceinline__ float dot4(float ax, float ay, float az, float aw, float bx, float by, float bz, float bw) {
   float r = ax * bx;
@@ -53,10 +52,10 @@ __device__ __forceinline__ void mul_point(const float* m, float x, float y, floa
   o[3] = __fdiv_rn(0.0f, d);
 }
 
-// InitTracingFrame for pixel (x, y).
-__device__ __forceinline__ void init_ray(const TraceParams& p, int x, int y, float4& o, float4& d) {
-  const float* m = p.m;
-  const int W = p.width, H = p.height;
+// InitTracingFrame for pixel (x, y) of view v.
+__device__ __forceinline__ void init_ray(const ViewDesc& v, int x, int y, float4& o, float4& d) {
+  const float* m = v.m;
+  const int W = v.width, H = v.height;
   float ox = __fdiv_rn(m[2], m[14]), oy = __fdiv_rn(m[6], m[14]), oz = __fdiv_rn(m[10], m[14]);
   float ow = __fdiv_rn(0.0f, m[14]);
   float q[4];
@@ -73,27 +72,88 @@ __device__ __forceinline__ void init_ray(const TraceParams& p, int x, int y, flo
   float bx = ox - p1[0], by = oy - p1[1], bz = oz - p1[2], bw = ow - p1[3];
   float dist12 = __fsqrt_rn(dot4(ax, ay, az, aw, ax, ay, az, aw));
   float dist01 = __fsqrt_rn(dot4(bx, by, bz, bw, bx, by, bz, bw));
-  float coef = __fdiv_rn(p.lod * dist12, dist01);
+  float coef = __fdiv_rn(v.lod * dist12, dist01);
   o = make_float4(ox, oy, oz, 0.0f);
   d = make_float4(dx, dy, dz, coef);
 }
 
-__device__ __forceinline__ uint32_t ld_link(const uint32_t* links, uint32_t i) { return __ldg(links + i); }
+// CastRay (raycast.cl:33-256) split into cast_begin() (everything before its
+// while loop) and cast_run() (the loop, for a bounded number of iterations),
+// so a warp can stop its rays at a common point and hand idle lanes new rays.
+// The state is the reference's loop state; the outcome is encoded in it
+// (see Outcome) instead of extra result registers.
+struct Cast {
+  float tx_coef, ty_coef, tz_coef, tx_bias, ty_bias, tz_bias;
+  float t_min, t_max, h, px, py, pz, scale_exp2, coef, bias;
+  uint32_t parent, desc;
+  int idx, scale, octant, iter;
+};
 
-// CastRay: ESVO descent in [1,2]^3 over cache-format links; stops at a leaf,
-// at the LOD size, on a missing child block (fault), or after 300 iterations.
+// How cast_run left a ray.  kHit: node = parent, duplicate flag = bit 9 of
+// desc.  kFault: node = parent, t = t_min, block = desc >> 11.
+enum Outcome : int { kRunning = 0, kHit = 1, kFault = 2, kMiss = 3, kError = 4 };
+
+__device__ __forceinline__ void cast_begin(Cast& c, int root, float4 o, float4 d) {
+  float px0 = o.x + 1.0f, py0 = o.y + 1.0f, pz0 = o.z + 1.0f;
+  float dx = d.x, dy = d.y, dz = d.z;
+  c.coef = d.w;
+  c.bias = o.w;
+  if (fabsf(dx) < kEps) dx = copysignf(kEps, dx);
+  if (fabsf(dy) < kEps) dy = copysignf(kEps, dy);
+  if (fabsf(dz) < kEps) dz = copysignf(kEps, dz);
+  c.tx_coef = __fdiv_rn(1.0f, -fabsf(dx));
+  c.ty_coef = __fdiv_rn(1.0f, -fabsf(dy));
+  c.tz_coef = __fdiv_rn(1.0f, -fabsf(dz));
+  c.tx_bias = c.tx_coef * px0;
+  c.ty_bias = c.ty_coef * py0;
+  c.tz_bias = c.tz_coef * pz0;
+  c.octant = 0;
+  if (dx > 0.0f) c.octant ^= 1, c.tx_bias = 3.0f * c.tx_coef - c.tx_bias;
+  if (dy > 0.0f) c.octant ^= 2, c.ty_bias = 3.0f * c.ty_coef - c.ty_bias;
+  if (dz > 0.0f) c.octant ^= 4, c.tz_bias = 3.0f * c.tz_coef - c.tz_bias;
+  c.t_min = fmaxf(fmaxf(2.0f * c.tx_coef - c.tx_bias, 2.0f * c.ty_coef - c.ty_bias), 2.0f * c.tz_coef - c.tz_bias);
+  c.t_max = fminf(fminf(c.tx_coef - c.tx_bias, c.ty_coef - c.ty_bias), c.tz_coef - c.tz_bias);
+  c.h = c.t_max;
+  c.t_min = fmaxf(c.t_min, 0.0f);
+  c.parent = (uint32_t)root;
+  c.desc = 0;
+  c.idx = 0;
+  c.px = 1.0f;
+  c.py = 1.0f;
+  c.pz = 1.0f;
+  c.scale = kSMax - 1;
+  c.scale_exp2 = 0.5f;
+  if (1.5f * c.tx_coef - c.tx_bias > c.t_min) c.idx ^= 1, c.px = 1.5f;
+  if (1.5f * c.ty_coef - c.ty_bias > c.t_min) c.idx ^= 2, c.py = 1.5f;
+  if (1.5f * c.tz_coef - c.tz_bias > c.t_min) c.idx ^= 4, c.pz = 1.5f;
+  c.iter = 0;
+}
+
+// How a ray ended.  error: iteration limit or a corrupt cache; fault_block
+// != -1: the children of `node` are not loaded (t = where the ray stopped);
+// node == -1: miss; else a hit on `node` with the duplicate flag `dup`.
+struct RayEnd {
+  float t;
+  int node, fault_block, dup, error;
+  int iter;
+};
+
+// CastRay as one function over local state, for rays that run to their end
+// in one go (the one-thread-per-ray kernel).  The arithmetic and stack rules
+// are cast_begin + cast_run's; kept as a single loop with the reference's
+// shape because that form compiles to about 5% fewer warp instructions on
+// sm_103a than the resumable one.
 template <bool kCount>
-__device__ __forceinline__ Cast cast_ray(const TraceParams& p, float4 o, float4 d, uint32_t* fetches,
-                                         uint32_t* far_fetches, uint32_t* iters) {
-  Cast r;
+__device__ __forceinline__ RayEnd cast_ray(const TraceParams& p, float4 o, float4 d, uint32_t& fetches,
+                                           uint32_t& far_fetches) {
+  RayEnd r;
   r.fault_block = -1;
   r.error = 0;
   r.dup = 0;
-  float px0 = o.x + 1.0f, py0 = o.y + 1.0f, pz0 = o.z + 1.0f;
+  const float px0 = o.x + 1.0f, py0 = o.y + 1.0f, pz0 = o.z + 1.0f;
   float dx = d.x, dy = d.y, dz = d.z;
   const float coef = d.w, bias = o.w;
   uint2 stack[kSMax + 1];
-
   if (fabsf(dx) < kEps) dx = copysignf(kEps, dx);
   if (fabsf(dy) < kEps) dy = copysignf(kEps, dy);
   if (fabsf(dz) < kEps) dz = copysignf(kEps, dz);
@@ -105,14 +165,11 @@ __device__ __forceinline__ Cast cast_ray(const TraceParams& p, float4 o, float4 
   if (dx > 0.0f) octant ^= 1, tx_bias = 3.0f * tx_coef - tx_bias;
   if (dy > 0.0f) octant ^= 2, ty_bias = 3.0f * ty_coef - ty_bias;
   if (dz > 0.0f) octant ^= 4, tz_bias = 3.0f * tz_coef - tz_bias;
-
   float t_min = fmaxf(fmaxf(2.0f * tx_coef - tx_bias, 2.0f * ty_coef - ty_bias), 2.0f * tz_coef - tz_bias);
   float t_max = fminf(fminf(tx_coef - tx_bias, ty_coef - ty_bias), tz_coef - tz_bias);
   float h = t_max;
   t_min = fmaxf(t_min, 0.0f);
-
-  uint32_t parent = (uint32_t)p.root;
-  uint32_t desc = 0;
+  uint32_t parent = (uint32_t)p.root, desc = 0;
   int idx = 0;
   float px = 1.0f, py = 1.0f, pz = 1.0f;
   int scale = kSMax - 1;
@@ -120,24 +177,19 @@ __device__ __forceinline__ Cast cast_ray(const TraceParams& p, float4 o, float4 
   if (1.5f * tx_coef - tx_bias > t_min) idx ^= 1, px = 1.5f;
   if (1.5f * ty_coef - ty_bias > t_min) idx ^= 2, py = 1.5f;
   if (1.5f * tz_coef - tz_bias > t_min) idx ^= 4, pz = 1.5f;
-
   int iter = 0;
   while (scale < kSMax) {
     if (++iter > kIterLimit) {
       r.error = 1;
-      r.t = t_min;
-      r.node = (int)parent;
       break;
     }
     if (desc == 0) {
       if (parent >= p.node_limit) {  // only reachable from a corrupt cache
         r.error = 1;
-        r.t = t_min;
-        r.node = 0;
         break;
       }
-      desc = ld_link(p.links, parent);
-      if (kCount) ++*fetches;
+      desc = __ldg(p.links + parent);
+      if (kCount) ++fetches;
     }
     const float tx_corner = px * tx_coef - tx_bias;
     const float ty_corner = py * ty_coef - ty_bias;
@@ -155,25 +207,21 @@ __device__ __forceinline__ Cast cast_ray(const TraceParams& p, float4 o, float4 
       if (desc & (1u << 10)) {
         if ((desc >> 11) >= p.far_limit) {
           r.error = 1;
-          r.t = t_min;
-          r.node = (int)parent;
           break;
         }
         ofs = __ldg(p.far_ptrs + (desc >> 11));
-        if (kCount) ++*far_fetches;
+        if (kCount) ++far_fetches;
       } else {
         ofs = (desc >> 11) + parent - (1u << 20);
       }
       ofs += __popc(desc & (bit - 1) & 255u);
       if (ofs >= p.node_limit) {
         r.error = 1;
-        r.t = t_min;
-        r.node = (int)parent;
         break;
       }
-      desc = ld_link(p.links, ofs);
-      if (kCount) ++*fetches;
-      if (!(desc & 255u) || tc_max * coef + bias >= scale_exp2) {
+      desc = __ldg(p.links + ofs);
+      if (kCount) ++fetches;
+      if (!(desc & 255u) || scale == 0 || tc_max * coef + bias >= scale_exp2) {
         r.t = t_min;
         r.node = (int)ofs;
         r.dup = (int)((desc >> 9) & 1u);
@@ -206,10 +254,7 @@ __device__ __forceinline__ Cast cast_ray(const TraceParams& p, float4 o, float4 
       if (step & 1) diff |= (uint32_t)(__float_as_int(px) ^ __float_as_int(px + scale_exp2));
       if (step & 2) diff |= (uint32_t)(__float_as_int(py) ^ __float_as_int(py + scale_exp2));
       if (step & 4) diff |= (uint32_t)(__float_as_int(pz) ^ __float_as_int(pz + scale_exp2));
-      // (float)diff is exact (diff < 2^23), so its exponent is the top bit
       scale = (__float_as_int((float)diff) >> 23) - 127;
-      // popping past the root: the loop ends here (the reference reads one
-      // more stack entry first, whose value it never uses)
       if (scale >= kSMax) break;
       scale_exp2 = __int_as_float((scale - kSMax + 127) << 23);
       const uint2 e = stack[scale];
@@ -226,12 +271,141 @@ __device__ __forceinline__ Cast cast_ray(const TraceParams& p, float4 o, float4 
       desc = 0;
     }
   }
-  if (scale >= kSMax && !r.error && r.fault_block == -1) {
-    r.t = 1e30f;
-    r.node = -1;
-  }
-  if (kCount) *iters = (uint32_t)iter;
+  if (scale >= kSMax && !r.error && r.fault_block == -1) r.node = -1;  // left the octree: miss
+  r.iter = iter;
   return r;
+}
+
+// CastRay's loop until the ray ends or (kBudget) its iteration count reaches
+// `stop` <= kIterLimit (kRunning: the ray continues from there on the next
+// call).  The loop runs on local copies of the state, written back once at
+// the end, and leaves through one exit.
+// A node at scale 0 ends the ray like a leaf: its children would lie below
+// float resolution and below the stack, which only a tree deeper than 23
+// levels reaches (the reference reads and writes past its stack there).  So
+// every stack index stays in [0, 22].
+template <bool kCount, bool kBudget>
+__device__ __forceinline__ int cast_run(Cast& c, int stop, uint2* stack, const TraceParams& p, uint32_t& fetches,
+                                        uint32_t& far_fetches) {
+  const float tx_coef = c.tx_coef, ty_coef = c.ty_coef, tz_coef = c.tz_coef;
+  const float tx_bias = c.tx_bias, ty_bias = c.ty_bias, tz_bias = c.tz_bias;
+  const float coef = c.coef, bias = c.bias;
+  const int octant = c.octant;
+  float t_min = c.t_min, t_max = c.t_max, h = c.h, px = c.px, py = c.py, pz = c.pz, scale_exp2 = c.scale_exp2;
+  uint32_t parent = c.parent, desc = c.desc;
+  int idx = c.idx, scale = c.scale, iter = c.iter;
+  int outcome = kMiss;
+  while (scale < kSMax) {
+    if (++iter > (kBudget ? stop : kIterLimit)) {
+      if (!kBudget || iter > kIterLimit) {
+        outcome = kError;
+      } else {
+        --iter;
+        outcome = kRunning;
+      }
+      break;
+    }
+    if (desc == 0) {
+      if (parent >= p.node_limit) {  // only reachable from a corrupt cache
+        outcome = kError;
+        break;
+      }
+      desc = __ldg(p.links + parent);
+      if (kCount) ++fetches;
+    }
+    const float tx_corner = px * tx_coef - tx_bias;
+    const float ty_corner = py * ty_coef - ty_bias;
+    const float tz_corner = pz * tz_coef - tz_bias;
+    const float tc_max = fminf(fminf(tx_corner, ty_corner), tz_corner);
+    const uint32_t bit = 1u << (idx ^ octant);
+    if ((desc & bit) != 0 && t_min <= t_max) {
+      if (desc & (1u << 8)) {  // children not loaded
+        outcome = kFault;
+        break;
+      }
+      uint32_t ofs;
+      if (desc & (1u << 10)) {
+        if ((desc >> 11) >= p.far_limit) {
+          outcome = kError;
+          break;
+        }
+        ofs = __ldg(p.far_ptrs + (desc >> 11));
+        if (kCount) ++far_fetches;
+      } else {
+        ofs = (desc >> 11) + parent - (1u << 20);
+      }
+      ofs += __popc(desc & (bit - 1) & 255u);
+      if (ofs >= p.node_limit) {
+        outcome = kError;
+        break;
+      }
+      desc = __ldg(p.links + ofs);
+      if (kCount) ++fetches;
+      if (!(desc & 255u) || scale == 0 || tc_max * coef + bias >= scale_exp2) {
+        parent = ofs;
+        outcome = kHit;
+        break;
+      }
+      const float half = scale_exp2 * 0.5f;
+      const float tx_center = half * tx_coef + tx_corner;
+      const float ty_center = half * ty_coef + ty_corner;
+      const float tz_center = half * tz_coef + tz_corner;
+      if (tc_max < h) stack[scale] = make_uint2(parent, __float_as_uint(t_max));
+      h = tc_max;
+      parent = ofs;
+      idx = 0;
+      --scale;
+      scale_exp2 = half;
+      if (tx_center > t_min) idx ^= 1, px = px + scale_exp2;
+      if (ty_center > t_min) idx ^= 2, py = py + scale_exp2;
+      if (tz_center > t_min) idx ^= 4, pz = pz + scale_exp2;
+      t_max = tc_max;
+      continue;
+    }
+    int step = 0;
+    if (tx_corner <= tc_max) step ^= 1, px = px - scale_exp2;
+    if (ty_corner <= tc_max) step ^= 2, py = py - scale_exp2;
+    if (tz_corner <= tc_max) step ^= 4, pz = pz - scale_exp2;
+    t_min = tc_max;
+    idx ^= step;
+    if ((idx & step) != 0) {
+      uint32_t diff = 0;
+      if (step & 1) diff |= (uint32_t)(__float_as_int(px) ^ __float_as_int(px + scale_exp2));
+      if (step & 2) diff |= (uint32_t)(__float_as_int(py) ^ __float_as_int(py + scale_exp2));
+      if (step & 4) diff |= (uint32_t)(__float_as_int(pz) ^ __float_as_int(pz + scale_exp2));
+      // (float)diff is exact (diff < 2^23), so its exponent is the top bit
+      scale = (__float_as_int((float)diff) >> 23) - 127;
+      // popping past the root ends the loop (the reference reads one more
+      // stack entry first, whose value it never uses)
+      if (scale >= kSMax) break;
+      scale_exp2 = __int_as_float((scale - kSMax + 127) << 23);
+      const uint2 e = stack[scale];
+      parent = e.x;
+      t_max = __uint_as_float(e.y);
+      const uint32_t shx = __float_as_uint(px) >> scale;
+      const uint32_t shy = __float_as_uint(py) >> scale;
+      const uint32_t shz = __float_as_uint(pz) >> scale;
+      px = __uint_as_float(shx << scale);
+      py = __uint_as_float(shy << scale);
+      pz = __uint_as_float(shz << scale);
+      idx = (int)((shx & 1u) | ((shy & 1u) << 1) | ((shz & 1u) << 2));
+      h = 0.0f;
+      desc = 0;
+    }
+  }
+  c.t_min = t_min;
+  c.t_max = t_max;
+  c.h = h;
+  c.px = px;
+  c.py = py;
+  c.pz = pz;
+  c.scale_exp2 = scale_exp2;
+  c.parent = parent;
+  c.desc = desc;
+  c.idx = idx;
+  c.scale = scale;
+  c.iter = iter;
+  return outcome;
 }
 
 // ProcessHit: fixed ambient + three directional lights; returns RGBA8 (A=255).
@@ -298,8 +472,7 @@ __device__ __forceinline__ void warp_set_bit(uint32_t* bits, int bit) {
   const int word = bit >= 0 ? (bit >> 5) : -1;
   const unsigned peers = __match_any_sync(active, word);
   if (word < 0) return;
-  unsigned m = 1u << (bit & 31);
-  // OR together the bits of all lanes that share the word
+  const unsigned m = 1u << (bit & 31);
   unsigned acc = 0;
   unsigned rest = peers;
   while (rest) {
@@ -313,73 +486,176 @@ __device__ __forceinline__ void warp_set_bit(uint32_t* bits, int bit) {
   }
 }
 
-template <bool kFirst, bool kCount>
-__global__ void __launch_bounds__(kBlockThreads) trace_kernel(const __grid_constant__ TraceParams p) {
-  int pixel, x = 0, y = 0;
-  float4 o, d;
+// View of the launch holding tile `tile` (tile_base is ascending).
+__device__ __forceinline__ int view_of_tile(const TraceParams& p, int tile) {
+  int lo = 0, hi = p.n_views - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (p.views[mid].tile_base <= tile) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Pixel (x, y) and view of first-pass ray r (tile r / 32, lane r % 32);
+// false for the lanes of a partial tile that fall outside the view.
+__device__ __forceinline__ bool first_pass_pixel(const TraceParams& p, int r, int& v, int& x, int& y) {
+  const int tile = (int)(r >> 5), k = (int)(r & 31);
+  v = view_of_tile(p, tile);
+  const ViewDesc& vd = p.views[v];
+  const int t = tile - vd.tile_base;
+  x = ((t % vd.tiles_x) << p.tile_w_log2) + (k & ((1 << p.tile_w_log2) - 1));
+  y = (t / vd.tiles_x) * (32 >> p.tile_w_log2) + (k >> p.tile_w_log2);
+  return x < vd.width && y < vd.height;
+}
+
+// kBudget: warps stop their rays every step_budget iterations and refill idle
+// lanes once `refill` of them are idle; otherwise a warp takes new rays once
+// all 32 ended.
+// Ray r of the launch (first pass: tile r / 32 of the views; later passes:
+// record r of the input list): its pixel, origin and direction; false for
+// the lanes of a partial tile that fall outside their view.
+template <bool kFirst>
+__device__ __forceinline__ bool ray_at(const TraceParams& p, int r, uint32_t& ray, float4& o, float4& d) {
   if (kFirst) {
-    // CTA = 4 x 8 warps; each warp covers an 8 x 4 pixel tile
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int tiles_x = (p.width + kTileW - 1) / kTileW;
-    const int tile = blockIdx.x * (kBlockThreads / 32) + warp;
-    x = (tile % tiles_x) * kTileW + (lane & (kTileW - 1));
-    y = (tile / tiles_x) * kTileH + (lane / kTileW);
-    if (x >= p.width || y >= p.height) return;
-    pixel = y * p.width + x;
-    init_ray(p, x, y, o, d);
+    int v, x, y;
+    if (!first_pass_pixel(p, r, v, x, y)) return false;
+    const ViewDesc& vd = p.views[v];
+    init_ray(vd, x, y, o, d);
+    ray = (uint32_t)(vd.pix_base + y * vd.width + x);
   } else {
-    const int i = blockIdx.x * kBlockThreads + threadIdx.x;
-    if (i >= *p.n_active_in) return;
-    pixel = p.active_in[i];
-    o = p.origin[pixel];
-    d = p.dir[pixel];
+    o = p.in_origin[r];
+    d = p.in_dir[r];
+    ray = p.in_ray[r];
   }
+  return true;
+}
 
-  uint32_t fetches = 0, far_fetches = 0, iters = 0;
-  const Cast c = cast_ray<kCount>(p, o, d, &fetches, &far_fetches, &iters);
-
+// RaytracingPass's handling of an ended ray (raytracing_pass.cl:20-58) plus
+// FinishTracingFrame for rays that end here: the final pixel, the next pass's
+// record of a faulted ray, the feedback bitmaps and counters.  Called by the
+// lanes whose rays ended, together.
+template <bool kCount>
+__device__ __forceinline__ void end_ray(const TraceParams& p, const RayEnd& e, uint32_t ray, float4 o, const float4 d,
+                                        uint32_t fetches, uint32_t far_fetches) {
+  const int lane = threadIdx.x & 31;
+  const bool faulted = !e.error && e.fault_block != -1;
+  const bool hit = !e.error && e.fault_block == -1 && e.node != -1;
+  const int node = e.node, dup = e.dup, fault_block = e.fault_block;
   int32_t word = kNoHit;
-  bool faulted = false;
-  if (c.error) {
-    p.image[pixel] = finish(p, make_uchar4(255, 0, 0, 255));
-  } else if (c.fault_block != -1) {
-    faulted = true;
-    o.x = o.x + d.x * c.t;
-    o.y = o.y + d.y * c.t;
-    o.z = o.z + d.z * c.t;
-    o.w = o.w + d.w * c.t;
-    p.origin[pixel] = o;
-    if (kFirst) p.dir[pixel] = d;
-    p.fault_parent[pixel] = c.node;
-    word = -c.fault_block - 1;
-  } else if (c.node == -1) {
-    p.image[pixel] = finish(p, make_uchar4(0, 0, 0, 0));
+  if (e.error) {
+    p.image[ray] = finish(p, make_uchar4(255, 0, 0, 255));
+  } else if (faulted) {
+    word = -fault_block - 1;
+  } else if (!hit) {
+    p.image[ray] = finish(p, make_uchar4(0, 0, 0, 0));
   } else {
-    const uchar4 col = (p.normals && p.colors) ? shade(p, c.node) : make_uchar4(0, 0, 0, 0);
-    p.image[pixel] = finish(p, col);
-    word = (int32_t)(((uint32_t)(c.node + 1) << 1) | (uint32_t)c.dup);
+    const uchar4 col = (p.normals && p.colors) ? shade(p, node) : make_uchar4(0, 0, 0, 0);
+    p.image[ray] = finish(p, col);
+    word = (int32_t)(((uint32_t)(node + 1) << 1) | (uint32_t)dup);
   }
-  if (p.words_dense) p.words_dense[pixel] = word;
-
-  // next pass's active list
-  const int slot = warp_append(p.n_active_out, faulted);
-  if (faulted) p.active_out[slot] = pixel;
-  // feedback bitmaps (NodeToBlock applied: hits are per cache block)
-  const bool is_hit = word != kNoHit && word > 0;
-  warp_set_bit(p.fault_bits, faulted && c.fault_block < p.fault_bit_limit ? c.fault_block : -1);
-  warp_set_bit(p.hit_bits, is_hit ? 2 * (c.node / p.nodes_in_block) + c.dup : -1);
+  if (p.words_dense) p.words_dense[ray] = word;
+  const int slot = warp_append(p.n_out, faulted);
+  if (faulted) {  // origin moved to the fault
+    o.x = o.x + d.x * e.t;
+    o.y = o.y + d.y * e.t;
+    o.z = o.z + d.z * e.t;
+    o.w = o.w + d.w * e.t;
+    p.out_origin[slot] = o;
+    p.out_dir[slot] = d;
+    p.out_parent[slot] = node;
+    p.out_ray[slot] = ray;
+  }
+  warp_set_bit(p.fault_bits, faulted && fault_block < p.fault_bit_limit ? fault_block : -1);
+  warp_set_bit(p.hit_bits, hit ? 2 * (node / p.nodes_in_block) + dup : -1);
   {
     const unsigned active = __activemask();
     const unsigned m = __ballot_sync(active, word != kNoHit);
-    if (m && (threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(p.n_words, __popc(m));
+    if (m && lane == __ffs(m) - 1) atomicAdd(p.n_words, __popc(m));
   }
   if (kCount) {
-    const unsigned v[6] = {1u, fetches, far_fetches, iters, is_hit ? 1u : 0u, faulted ? 1u : 0u};
+    const unsigned v[6] = {1u, fetches, far_fetches, (unsigned)e.iter, hit ? 1u : 0u, faulted ? 1u : 0u};
     const unsigned active = __activemask();
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
-      const unsigned s = __reduce_add_sync(active, v[k]);
-      if ((threadIdx.x & 31) == __ffs(active) - 1) atomicAdd(p.counters + k, (unsigned long long)s);
+      const unsigned sum = __reduce_add_sync(active, v[k]);
+      if (lane == __ffs(active) - 1) atomicAdd(p.counters + k, (unsigned long long)sum);
+    }
+  }
+}
+
+// One ray per thread over a grid that covers the launch's rays (a warp = one
+// 32-ray tile); the hardware hands CTAs to SMs as earlier ones retire.
+template <bool kFirst, bool kCount>
+__global__ void __launch_bounds__(kBlockThreads) trace_kernel(const __grid_constant__ TraceParams p) {
+  const int total = kFirst ? p.total_tiles * 32 : *p.n_in;
+  const int r = blockIdx.x * kBlockThreads + threadIdx.x;
+  if (r >= total) return;
+  uint32_t ray;
+  float4 o, d;
+  if (!ray_at<kFirst>(p, r, ray, o, d)) return;
+  uint32_t fetches = 0, far_fetches = 0;
+  const RayEnd e = cast_ray<kCount>(p, o, d, fetches, far_fetches);
+  end_ray<kCount>(p, e, ray, o, d, fetches, far_fetches);
+}
+
+// Persistent form: one CTA per SM slot; every warp takes rays from the
+// launch's work counter.  A warp runs its rays for step_budget iterations at a
+// time and, once at least `refill` of its lanes sit idle (refill = 32: all of
+// them), hands those lanes the next rays, so lanes do not idle through the
+// warp's longest ray.  Once the counter is exhausted the rays run to the end.
+template <bool kFirst, bool kCount>
+__global__ void __launch_bounds__(kBlockThreads) trace_persistent_kernel(const __grid_constant__ TraceParams p) {
+  __shared__ float4 s_origin[kBlockThreads], s_dir[kBlockThreads];
+  const int lane = threadIdx.x & 31;
+  const int total = kFirst ? p.total_tiles * 32 : *p.n_in;  // below 2^31: at most 2^30 pixels
+  uint2 stack[kSMax + 1];
+  Cast c;
+  int outcome = kRunning;
+  uint32_t ray = 0;
+  bool have = false, exhausted = false;
+  uint32_t fetches = 0, far_fetches = 0;
+
+  for (;;) {
+    const unsigned idle = __ballot_sync(kFull, !have);
+    if (!exhausted && __popc(idle) >= p.refill) {
+      const int want = __popc(idle);
+      const int leader = __ffs(idle) - 1;
+      int base = 0;
+      if (lane == leader) base = atomicAdd(p.work, want);
+      base = __shfl_sync(kFull, base, leader);
+      if (base + want >= total) exhausted = true;
+      if (!have) {
+        const int r = base + __popc(idle & ((1u << lane) - 1));
+        float4 o, d;
+        if (r < total && ray_at<kFirst>(p, r, ray, o, d)) {
+          s_origin[threadIdx.x] = o;  // kept for the ray's fault record
+          s_dir[threadIdx.x] = d;
+          cast_begin(c, p.root, o, d);
+          have = true;
+          fetches = far_fetches = 0;
+        }
+      }
+    }
+    if (!__ballot_sync(kFull, have)) {
+      if (exhausted) break;
+      continue;
+    }
+    if (have && outcome == kRunning) {
+      const int stop = exhausted ? kIterLimit : min(c.iter + p.step_budget, kIterLimit);
+      outcome = cast_run<kCount, true>(c, stop, stack, p, fetches, far_fetches);
+    }
+    if (outcome != kRunning) {
+      RayEnd e;
+      e.t = c.t_min;
+      e.node = outcome == kMiss ? -1 : (int)c.parent;
+      e.fault_block = outcome == kFault ? (int)(c.desc >> 11) : -1;
+      e.dup = (int)((c.desc >> 9) & 1u);
+      e.error = outcome == kError;
+      e.iter = c.iter;
+      end_ray<kCount>(p, e, ray, s_origin[threadIdx.x], s_dir[threadIdx.x], fetches, far_fetches);
+      have = false;
+      outcome = kRunning;
     }
   }
 }
@@ -388,10 +664,9 @@ __global__ void __launch_bounds__(kBlockThreads) trace_kernel(const __grid_const
 // with the fault's parent node as the cache holds it now.
 __global__ void __launch_bounds__(kBlockThreads) finish_kernel(const __grid_constant__ TraceParams p) {
   const int i = blockIdx.x * kBlockThreads + threadIdx.x;
-  if (i >= *p.n_active_in) return;
-  const int pixel = p.active_in[i];
-  const uchar4 col = (p.normals && p.colors) ? shade(p, p.fault_parent[pixel]) : make_uchar4(0, 0, 0, 0);
-  p.image[pixel] = finish(p, col);
+  if (i >= *p.n_in) return;
+  const uchar4 col = (p.normals && p.colors) ? shade(p, p.in_parent[i]) : make_uchar4(0, 0, 0, 0);
+  p.image[p.in_ray[i]] = finish(p, col);
 }
 
 __global__ void fill_kernel(int* p, int32_t v, size_t n) {
@@ -404,6 +679,7 @@ __global__ void fill_kernel(int* p, int32_t v, size_t n) {
 constexpr int kUniqThreads = 1024;
 __global__ void __launch_bounds__(kUniqThreads) unique_from_bits_kernel(const UniqueFromBitsParams q) {
   __shared__ int warp_sums[32];
+  __shared__ int fsum;
   const int total = q.fault_words + q.hit_words;
   const int per = (total + kUniqThreads - 1) / kUniqThreads;
   const int begin = min(total, (int)threadIdx.x * per), end = min(total, begin + per);
@@ -412,24 +688,24 @@ __global__ void __launch_bounds__(kUniqThreads) unique_from_bits_kernel(const Un
   };
   int cnt = 0, fcnt = 0;
   for (int k = begin; k < end; ++k) {
-    const int c = __popc(word_at(k));
-    cnt += c;
-    if (k < q.fault_words) fcnt += c;
+    const int n = __popc(word_at(k));
+    cnt += n;
+    if (k < q.fault_words) fcnt += n;
   }
-  // block exclusive scan of cnt (and a reduction of fcnt)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int incl = cnt;
   for (int off = 1; off < 32; off <<= 1) {
-    int v = __shfl_up_sync(0xffffffffu, incl, off);
+    int v = __shfl_up_sync(kFull, incl, off);
     if (lane >= off) incl += v;
   }
   if (lane == 31) warp_sums[warp] = incl;
+  if (threadIdx.x == 0) fsum = 0;
   __syncthreads();
   if (warp == 0) {
     int v = warp_sums[lane];
     int s = v;
     for (int off = 1; off < 32; off <<= 1) {
-      int u = __shfl_up_sync(0xffffffffu, s, off);
+      int u = __shfl_up_sync(kFull, s, off);
       if (lane >= off) s += u;
     }
     warp_sums[lane] = s - v;  // exclusive
@@ -454,42 +730,58 @@ __global__ void __launch_bounds__(kUniqThreads) unique_from_bits_kernel(const Un
       }
     }
   }
-  // totals
   int f = fcnt;
-  for (int off = 16; off > 0; off >>= 1) f += __shfl_down_sync(0xffffffffu, f, off);
-  __shared__ int fsum;
-  if (threadIdx.x == 0) fsum = 0;
-  __syncthreads();
+  for (int off = 16; off > 0; off >>= 1) f += __shfl_down_sync(kFull, f, off);
   if (lane == 0) atomicAdd(&fsum, f);
   __syncthreads();
   if (threadIdx.x == kUniqThreads - 1) {
-    int n = pos;  // last thread's end position = total set bits
+    int n = pos;  // the last thread's end position = total set bits
     if (*q.n_words < q.total_pixels) q.unique_out[n++] = kNoHit;
     q.counts_out[0] = n;
     q.counts_out[1] = fsum;
+    q.counts_out[2] = q.n_rays ? *q.n_rays : 0;
   }
 }
 
-}  // namespace
+template <bool kFirst, bool kCount>
+int persistent_grid() {
+  static int grid = 0;
+  if (!grid) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_persistent_kernel<kFirst, kCount>, kBlockThreads, 0);
+    grid = sms * (per_sm > 0 ? per_sm : 1);
+  }
+  return grid;
+}
 
-cudaError_t launch_trace(const TraceParams& p, bool first, bool count, int max_active, cudaStream_t s) {
-  if (first) {
-    const int tiles = ((p.width + kTileW - 1) / kTileW) * ((p.height + kTileH - 1) / kTileH);
-    const int grid = (tiles + (kBlockThreads / 32) - 1) / (kBlockThreads / 32);
-    if (count) trace_kernel<true, true><<<grid, kBlockThreads, 0, s>>>(p);
-    else trace_kernel<true, false><<<grid, kBlockThreads, 0, s>>>(p);
+template <bool kFirst, bool kCount>
+cudaError_t launch_variant(const TraceParams& p, int rays, int grid, cudaStream_t s) {
+  if (p.refill < 32) {
+    trace_persistent_kernel<kFirst, kCount><<<grid, kBlockThreads, 0, s>>>(p);
   } else {
-    if (max_active <= 0) return cudaSuccess;
-    const int grid = (max_active + kBlockThreads - 1) / kBlockThreads;
-    if (count) trace_kernel<false, true><<<grid, kBlockThreads, 0, s>>>(p);
-    else trace_kernel<false, false><<<grid, kBlockThreads, 0, s>>>(p);
+    if (rays <= 0) return cudaSuccess;
+    trace_kernel<kFirst, kCount><<<(rays + kBlockThreads - 1) / kBlockThreads, kBlockThreads, 0, s>>>(p);
   }
   return cudaGetLastError();
 }
 
-cudaError_t launch_finish(const TraceParams& p, int max_active, cudaStream_t s) {
-  if (max_active <= 0) return cudaSuccess;
-  finish_kernel<<<(max_active + kBlockThreads - 1) / kBlockThreads, kBlockThreads, 0, s>>>(p);
+}  // namespace
+
+int trace_persistent_grid(bool first, bool count) {
+  if (first) return count ? persistent_grid<true, true>() : persistent_grid<true, false>();
+  return count ? persistent_grid<false, true>() : persistent_grid<false, false>();
+}
+
+cudaError_t launch_trace(const TraceParams& p, bool first, bool count, int rays, int grid, cudaStream_t s) {
+  if (first) return count ? launch_variant<true, true>(p, rays, grid, s) : launch_variant<true, false>(p, rays, grid, s);
+  return count ? launch_variant<false, true>(p, rays, grid, s) : launch_variant<false, false>(p, rays, grid, s);
+}
+
+cudaError_t launch_finish(const TraceParams& p, int max_rays, cudaStream_t s) {
+  if (max_rays <= 0) return cudaSuccess;
+  finish_kernel<<<(max_rays + kBlockThreads - 1) / kBlockThreads, kBlockThreads, 0, s>>>(p);
   return cudaGetLastError();
 }
 
