@@ -1,6 +1,6 @@
 """Benchmark of the per-frame path on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload c3|c1|c2]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload c3|c1|c2|c4]
 
 The default workload is c3, the configuration the Mrays/s-at-1080p metric is
 quoted on.
@@ -15,6 +15,9 @@ builder; no public dataset is involved):
       a seeded Catmull-Rom spline, block cache capped at 2 GiB, blocks
       streamed from the file
   c2  2^28 feedback words: 90% NO_HIT, Zipf(1.1) block IDs over 2^24
+  c4  the c3 scene, 64 views per frame of sizes drawn from {256^2, 640x480,
+      1280x720, 1920x1080} (seed 7), view v on its own spline (seed 7 + v),
+      through the batched renderer; the plain per-view path is timed beside it
 
 --impl reference times the reference algorithm's CPU implementation (the
 oracle restatement in oracle/, all host threads) on the same workload.
@@ -42,6 +45,10 @@ C1_CAMERA = [45.0, -30.0, 0.0, -0.06, 0.66, 1.06, 60.0]
 WORKLOADS = {
     "c1": {"depth": 10, "spheres": 0, "width": 512, "height": 512, "cache_bytes": 0, "lod": 1.0},
     "c3": {"depth": 12, "spheres": 2000, "width": 1920, "height": 1080, "cache_bytes": 2 << 30, "lod": 1.0},
+    # 64 views per frame; the cache holds the whole tree (about 6.5 GB), so a
+    # frame measures batched traversal + feedback rather than streaming
+    "c4": {"depth": 12, "spheres": 2000, "width": 0, "height": 0, "cache_bytes": 0, "lod": 1.0, "views": 64,
+           "sizes": [(256, 256), (640, 480), (1280, 720), (1920, 1080)], "size_seed": 7},
 }
 
 
@@ -51,7 +58,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=0)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3"])
+    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU baseline sample")
     ap.add_argument("--spheres", type=int, default=None, help="override the workload's sphere count")
     ap.add_argument("--cache-mib", type=int, default=None, help="override the workload's cache size")
@@ -195,15 +202,16 @@ def scene_path(wl, local_rank, world):
     return path
 
 
-def camera_path(wl, frames, w, h):
-    """C1: one fixed camera.  C3: a Catmull-Rom spline through 8 control points
-    drawn with seed 3 inside the scene, looking along the path and 25 deg down."""
+def camera_path(wl, frames, w, h, seed=3):
+    """C1: one fixed camera.  C3/C4: a Catmull-Rom spline through 8 control
+    points drawn with `seed` inside the scene, looking along the path and 25 deg
+    down (C3 seed 3; C4 view v seed 7 + v)."""
     import rayt_gb300 as R
     if wl == "c1":
         c = R.Camera(C1_CAMERA[0], C1_CAMERA[1], C1_CAMERA[2], C1_CAMERA[3:6], C1_CAMERA[6], w / h)
         m = c.view_proj_inv()
         return [m] * frames
-    rng = np.random.default_rng(3)
+    rng = np.random.default_rng(seed)
     pts = np.stack([rng.uniform(0.15, 0.85, 8), rng.uniform(0.62, 0.85, 8), rng.uniform(0.15, 0.85, 8)], 1)
     pts = np.concatenate([pts, pts[:3]])  # closed loop
 
@@ -381,6 +389,165 @@ def bench_frames(args, rank, world, local):
     }
 
 
+def batched_views(cfg):
+    """C4: view v's size (drawn uniformly with seed 7) and camera spline seed."""
+    rng = np.random.default_rng(cfg["size_seed"])
+    pick = rng.integers(0, len(cfg["sizes"]), size=cfg["views"])
+    return [tuple(cfg["sizes"][k]) for k in pick], [cfg["size_seed"] + v for v in range(cfg["views"])]
+
+
+def bench_batched(args, rank, world, local):
+    """C4: every frame renders 64 views of mixed sizes through one batched
+    renderer (rayt_render_views: one traversal launch per pass for all views,
+    pass graphs, launch shape from the autotuner).  Also times the same frames
+    through the plain per-frame path, one RenderFrame per view."""
+    import torch
+
+    import rayt_gb300 as R
+    wl = "c4"
+    cfg = WORKLOADS[wl]
+    steps = args.steps or 20
+    path = scene_path(wl, local, world)
+    sizes, seeds = batched_views(cfg)
+    n = len(sizes)
+    frames = args.warmup + steps
+    per_view = [camera_path(wl, frames, w, h, seed=sd) for (w, h), sd in zip(sizes, seeds)]
+    mats = [[per_view[v][f] for v in range(n)] for f in range(frames)]
+    rays_per_frame = sum(w * h for w, h in sizes)
+    threads = os.cpu_count() or 1
+    metric = "Mrays/s, 64 views per frame (batched form, depth 12)"
+
+    def cpu_frames(budget):
+        from oracle import oracle as O
+        sc = O.OracleScene(path, cache_blocks(cfg), views=sizes, lod=cfg["lod"])
+        el, k = 0.0, 0
+        for f in range(args.warmup, frames):
+            t = time.time()
+            sc.render_views(mats[f])
+            el += time.time() - t
+            k += 1
+            if el > budget:
+                break
+        sc.close()
+        return k * rays_per_frame, el, k
+
+    if args.impl == "reference":
+        if rank != 0:
+            return None
+        rays, el, k = cpu_frames(args.cpu_seconds * 3)
+        v = rays / el / 1e6
+        return {"metric": metric, "value": round(v, 3), "unit": "Mrays/s", "impl": "reference", "n_gpus": 1,
+                "steps": k, "warmup": 0, "ms_per_step": round(el / k * 1e3, 3), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": wl, "views": n, "rays_per_frame": rays_per_frame, "depth": cfg["depth"]},
+                "cpu_baseline": {"value": round(v, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                                 "sample": "%d frames of 64 views (oracle, OpenMP)" % k},
+                "e2e": {"value": round(v, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+    torch.cuda.set_device(local)
+    ld = R.StoredOctreeLoader(path)
+    cm = R.GPUOctreeCacheManager(cache_blocks(cfg), ld)
+    t0 = time.time()
+    cm.InitialFillCache()
+    fill_s = time.time() - t0
+    rt = R.GPURayTracer.views(cm, sizes)
+    rt.set_lod_voxel_size(cfg["lod"])
+    rt.set_frame_time_limit(1e30)
+    t0 = time.time()
+    shape = rt.autotune(mats[0], reps=1)
+    tune_s = time.time() - t0
+    stream = torch.cuda.ExternalStream(rt.stream_handle())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    pinned = [torch.empty((h, w, 4), dtype=torch.uint8).pin_memory() for w, h in sizes]
+    for f in range(args.warmup):
+        rt.RenderViews(mats[f])
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms_dev, wall, launches, passes, lat = 0.0, 0.0, 0, 0, []
+    for f in range(args.warmup, frames):
+        with torch.cuda.stream(stream):
+            flush.fill_(f & 255)
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t = time.perf_counter()
+        e0.record(stream)
+        rt.RenderViews(mats[f])
+        e1.record(stream)
+        for v in range(n):  # end to end: every view's image to pinned host memory
+            R._check(R.lib().rayt_renderer_read_view_image(rt._h, v, pinned[v].data_ptr(), pinned[v].numel()))
+        wall += time.perf_counter() - t
+        e1.synchronize()
+        d = e0.elapsed_time(e1)
+        ms_dev += d
+        lat.append(d)
+        st = rt.stats()
+        launches += st["kernel_launches"]
+        passes += st["passes"]
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    t_dev = max_over_ranks(ms_dev / 1e3, world)
+    t_wall = max_over_ranks(wall, world)
+    total_rays = sum_over_ranks(float(rays_per_frame * steps), world)
+
+    # the same frames through the plain path: one renderer per view size, one
+    # RenderFrame per view
+    plain = {}
+    for sz in set(sizes):
+        r1 = R.GPURayTracer(cm, sz[0], sz[1])
+        r1.set_lod_voxel_size(cfg["lod"])
+        r1.set_frame_time_limit(1e30)
+        plain[sz] = r1
+    for v in range(n):
+        plain[sizes[v]].RenderFrame(mats[0][v])
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for f in range(args.warmup, frames):
+        for v in range(n):
+            plain[sizes[v]].RenderFrame(mats[f][v])
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t
+
+    # roofline of the first pass over all views
+    fetch = rt.count_fetches(mats[frames - 1])
+    pass_ms = rt.time_pass(mats[frames - 1], 3)
+    alg_bytes = 4 * fetch["link_fetches"] + 4 * fetch["far_fetches"] + 16 * fetch["rays"]
+    achieved = alg_bytes / (pass_ms / 1e3) / 1e9
+    peak, peak_kind = hbm_peak()
+    cpu = None
+    if rank == 0:
+        crays, cel, ck = cpu_frames(args.cpu_seconds)
+        cpu = {"value": round(crays / cel / 1e6, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+               "sample": "%d frames of the 64 views (oracle, OpenMP)" % ck}
+    if rank != 0:
+        return None
+    lat_sorted = np.sort(np.array(lat))
+    return {
+        "metric": metric, "value": round(total_rays / t_dev / 1e6, 3), "unit": "Mrays/s", "n_gpus": world,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": round(t_dev / steps * 1e3, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": wl, "views": n, "rays_per_frame": rays_per_frame, "depth": cfg["depth"],
+                   "spheres": cfg["spheres"], "cache_blocks": cm.blocks()[1], "tree_blocks": ld.info.blocks_count,
+                   "sizes": {"%dx%d" % k: sizes.count(k) for k in sorted(set(sizes))},
+                   "launch_shape": list(shape), "autotune_s": round(tune_s, 2), "graphs": True,
+                   "l2": "flushed between frames (256 MiB write)", "initial_fill_s": round(fill_s, 2),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": round(total_rays / t_wall / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 64 * 16 * 4,
+                "d2h_bytes_per_step": rays_per_frame * 4},
+        "frame_latency_ms": {"p50": round(float(np.percentile(lat_sorted, 50)), 4),
+                             "p99": round(float(np.percentile(lat_sorted, 99)), 4)},
+        "plain_per_view": {"value": round(rays_per_frame * steps / t_plain / 1e6, 3), "unit": "Mrays/s",
+                           "note": "same frames, one RenderFrame per view (wall clock)"},
+        "frames": {"passes_per_frame": round(passes / steps, 3)},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+                     "kernel": "trace_kernel<first pass>, all 64 views", "launch_ms": round(pass_ms, 4),
+                     "bytes_per_ray": round(alg_bytes / fetch["rays"], 2)},
+        "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clk}
+
+
 # ---------------------------------------------------------------------------
 def zipf_words(n, seed=5, blocks=1 << 24, s=1.1):
     """C2 input: 90% NO_HIT, the rest block IDs ~ Zipf(s) over [0, blocks)
@@ -482,6 +649,8 @@ def main():
         rank, world, local = dist_setup(args.gpus)
     if args.workload == "c2":
         out = bench_c2(args, rank, world, local)
+    elif args.workload == "c4":
+        out = bench_batched(args, rank, world, local)
     else:
         out = bench_frames(args, rank, world, local)
     if rank == 0 and out is not None:

@@ -185,6 +185,10 @@ int rayt_renderer_set_max_passes(rayt_renderer* r, int max_passes);
  * srand(seed), which the reference's feedback extractor draws from
  * (ray-tracing-feedback-extractor.cpp:147). */
 int rayt_renderer_seed(rayt_renderer* r, uint32_t seed);
+/* Replay each pass's device work (feedback reset, traversal, feedback unique)
+ * from a CUDA graph built once per pass kind (default on; recording passes
+ * uses plain launches).  Results do not depend on it. */
+int rayt_renderer_use_graphs(rayt_renderer* r, int on);
 /* Keep each pass's dense per-pixel feedback words for rayt_renderer_pass_words. */
 int rayt_renderer_record_passes(rayt_renderer* r, int on);
 /* GPURayTracer::RenderFrame(camera) (gpu-ray-tracer.cpp:66-227), given the

@@ -119,6 +119,7 @@ def lib():
         "rayt_renderer_set_max_passes": (i32, [vp, i32]),
         "rayt_renderer_seed": (i32, [vp, u32]),
         "rayt_renderer_record_passes": (i32, [vp, i32]),
+        "rayt_renderer_use_graphs": (i32, [vp, i32]),
         "rayt_render_frame": (i32, [vp, C.POINTER(f32)]),
         "rayt_renderer_image": (i32, [vp, C.POINTER(vp)]),
         "rayt_renderer_stream": (i32, [vp, C.POINTER(vp)]),
@@ -362,6 +363,9 @@ class GPURayTracer:
 
     def seed(self, seed):
         _check(lib().rayt_renderer_seed(self._h, seed))
+
+    def use_graphs(self, on=True):
+        _check(lib().rayt_renderer_use_graphs(self._h, 1 if on else 0))
 
     def record_passes(self, on=True):
         _check(lib().rayt_renderer_record_passes(self._h, 1 if on else 0))

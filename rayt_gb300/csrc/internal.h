@@ -81,11 +81,16 @@ struct TraceParams {
   ViewDesc views[kViewsPerLaunch];
 };
 
-// first: rays come from the views' cameras; otherwise from the input list.
-// refill = 32: one thread per ray over `rays` threads (rays = total_tiles * 32
-// on the first pass, an upper bound of *n_in after it); refill < 32: the
-// persistent work-stealing kernel over `grid` CTAs.
+// first: rays come from the views' cameras (refill = 32: one thread per ray
+// over rays = total_tiles * 32 threads; refill < 32: the persistent
+// work-stealing kernel over `grid` CTAs, 0 = as many as are resident).
+// Otherwise the faulted rays of the input list, by a persistent kernel whose
+// warps take 32 rays at a time (the count is read on the device).
 cudaError_t launch_trace(const TraceParams& p, bool first, bool count, int rays, int grid, cudaStream_t s);
+// The same launch as a kernel node of a CUDA graph (args: room for one pointer;
+// p must stay valid until the node is added or updated).
+cudaError_t trace_node_params(const TraceParams* p, bool first, bool count, int rays, int grid, void** args,
+                              cudaKernelNodeParams* kp);
 // Resident CTAs of the persistent traversal kernel on the current device.
 int trace_persistent_grid(bool first, bool count);
 cudaError_t launch_finish(const TraceParams& p, int max_rays, cudaStream_t s);
@@ -104,6 +109,7 @@ struct UniqueFromBitsParams {
   int* counts_out;       // [0] unique count (incl. NO_HIT), [1] fault count, [2] *n_rays
 };
 cudaError_t launch_unique_from_bits(const UniqueFromBitsParams& p, cudaStream_t s);
+cudaError_t unique_node_params(const UniqueFromBitsParams* q, void** args, cudaKernelNodeParams* kp);
 
 // ---- radix sort / scan / unique -------------------------------------------------
 struct SortScratch {

@@ -56,6 +56,7 @@ class Renderer {
                          // measured frame, kept for the autotuner)
   int ctas_per_sm = 0;   // persistent kernel: 0 = as many as fit
   int step_budget = 16;  // persistent kernel: iterations between refill checks
+  bool use_graphs = true;  // replay each pass's device work from a CUDA graph
   int n_views() const { return (int)views_.size(); }
   uchar4* image(int v) const { return d_images_ + views_[v].pix_base; }
   cudaStream_t stream() const { return s_; }
@@ -95,11 +96,39 @@ class Renderer {
   void Decode(int count);
   int Prepare(int it);
   int Trace(int it, bool count, int rays);
+  UniqueFromBitsParams UniqueParams(int it) const;
+  int RunPass(int it, int rays, int* launches);
+  int PassGraph(int kind, int it);
   int groups() const { return (int)group_tiles_.size(); }
+
+  // One pass's device work (clear feedback state, traversal, unique) as a
+  // graph: kind 0 = first pass, 1 and 2 = later passes writing list 1 and 0.
+  // The first pass's traversal nodes get the frame's view matrices before
+  // every replay; later passes replay unchanged.
+  struct Graph {
+    cudaGraph_t graph = nullptr;  // kept: node handles refer to it
+    cudaGraphExec_t exec = nullptr;
+    std::vector<cudaGraphNode_t> trace_nodes;
+    TraceParams key;  // the parameters (without views) it was built with
+    int ctas = 0;     // and the persistent kernel's CTAs per SM
+  };
+  Graph graphs_[3];
+  void DropGraphs();
 };
+
+void Renderer::DropGraphs() {
+  for (auto& g : graphs_) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (g.graph) cudaGraphDestroy(g.graph);
+    g.exec = nullptr;
+    g.graph = nullptr;
+    g.trace_nodes.clear();
+  }
+}
 
 Renderer::~Renderer() {
   if (s_) cudaStreamSynchronize(s_);
+  DropGraphs();
   cudaFree(d_images_);
   for (auto& l : lists_) {
     cudaFree(l.origin);
@@ -310,6 +339,119 @@ int Renderer::Trace(int it, bool count, int rays) {
   return RAYT_OK;
 }
 
+UniqueFromBitsParams Renderer::UniqueParams(int it) const {
+  UniqueFromBitsParams q{};
+  q.fault_bits = reinterpret_cast<const uint32_t*>(d_state_ + kBlockInts);
+  q.fault_words = fault_words_;
+  q.hit_bits = reinterpret_cast<const uint32_t*>(d_state_ + kBlockInts + fault_words_);
+  q.hit_words = hit_words_;
+  q.n_words = block(it & 1);
+  q.n_rays = block(it & 1) + 1;
+  q.total_pixels = total_pixels_;
+  q.unique_out = d_unique_;
+  q.counts_out = d_counts_;
+  return q;
+}
+
+// Builds (when missing or when the pass parameters changed) and updates the
+// graph of pass kind `kind`, then launches it.  Events 1 (after traversal)
+// and 2 (after unique) are recorded inside the graph.
+int Renderer::PassGraph(int kind, int it) {
+  Graph& g = graphs_[kind];
+  TraceParams key = Params(it);
+  if (g.exec && (std::memcmp(&key, &g.key, sizeof(key)) != 0 || g.ctas != ctas_per_sm)) {
+    cudaGraphExecDestroy(g.exec);
+    cudaGraphDestroy(g.graph);
+    g.exec = nullptr;
+    g.graph = nullptr;
+    g.trace_nodes.clear();
+  }
+  const bool first = kind == 0;
+  // per launch group (first pass) or one (later passes): parameters with views
+  std::vector<TraceParams> tp(first ? groups() : 1, key);
+  if (first) {
+    for (int grp = 0; grp < groups(); ++grp) {
+      TraceParams& p = tp[grp];
+      const int v0 = grp * kViewsPerLaunch, v1 = std::min(n_views(), v0 + kViewsPerLaunch);
+      p.n_views = v1 - v0;
+      std::memcpy(p.views, views_.data() + v0, (size_t)p.n_views * sizeof(ViewDesc));
+      p.total_tiles = group_tiles_[grp];
+      p.work = block(0) + 4 + grp;
+    }
+  }
+  const int grid = refill < 32 ? Grid(first, false) : 0;
+  void* args[1];
+  cudaKernelNodeParams kp;
+  if (!g.exec) {
+    cudaGraph_t graph;
+    RAYT_CUDA_TRY(cudaGraphCreate(&graph, 0));
+    cudaGraphNode_t prev = nullptr, node = nullptr;
+    cudaMemsetParams mp{};
+    mp.dst = (it & 1) ? d_state_ + kBlockInts : d_state_;
+    mp.value = 0;
+    mp.elementSize = 4;
+    mp.width = kBlockInts + (size_t)fault_words_ + hit_words_;
+    mp.height = 1;
+    cudaError_t e = cudaGraphAddMemsetNode(&node, graph, nullptr, 0, &mp);
+    prev = node;
+    for (size_t i = 0; e == cudaSuccess && i < tp.size(); ++i) {
+      trace_node_params(&tp[i], first, false, first ? group_tiles_[i] * 32 : 0, grid, args, &kp);
+      e = cudaGraphAddKernelNode(&node, graph, &prev, 1, &kp);
+      g.trace_nodes.push_back(node);
+      prev = node;
+    }
+    if (e == cudaSuccess) e = cudaGraphAddEventRecordNode(&node, graph, &prev, 1, ev_[1]);
+    prev = node;
+    const UniqueFromBitsParams q = UniqueParams(it);
+    if (e == cudaSuccess) {
+      unique_node_params(&q, args, &kp);
+      e = cudaGraphAddKernelNode(&node, graph, &prev, 1, &kp);
+      prev = node;
+    }
+    if (e == cudaSuccess) e = cudaGraphAddEventRecordNode(&node, graph, &prev, 1, ev_[2]);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&g.exec, graph, 0);
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(graph);
+      g.exec = nullptr;
+      g.trace_nodes.clear();
+      return cuda_fail(e, "pass graph construction");
+    }
+    g.graph = graph;
+    g.key = key;
+    g.ctas = ctas_per_sm;
+  } else if (first) {
+    for (size_t i = 0; i < tp.size(); ++i) {
+      trace_node_params(&tp[i], true, false, group_tiles_[i] * 32, grid, args, &kp);
+      RAYT_CUDA_TRY(cudaGraphExecKernelNodeSetParams(g.exec, g.trace_nodes[i], &kp));
+    }
+  }
+  RAYT_CUDA_TRY(cudaGraphLaunch(g.exec, s_));
+  return RAYT_OK;
+}
+
+// The device work of pass `it` over `rays` rays (traversal and feedback
+// unique, with events 0..2 around them); adds the kernels it launched.
+int Renderer::RunPass(int it, int rays, int* launches) {
+  RAYT_CUDA_TRY(cudaEventRecord(ev_[0], s_));
+  if (use_graphs && !record) {
+    int rc = PassGraph(it == 0 ? 0 : ((it & 1) ? 1 : 2), it);
+    if (rc != RAYT_OK) return rc;
+    *launches += (it == 0 ? groups() : 1) + 1;
+    return RAYT_OK;
+  }
+  int rc = Prepare(it);
+  if (rc != RAYT_OK) return rc;
+  if (it == 0 || rays > 0) {
+    if ((rc = Trace(it, false, rays)) != RAYT_OK) return rc;
+    *launches += it == 0 ? groups() : 1;
+  }
+  RAYT_CUDA_TRY(cudaEventRecord(ev_[1], s_));
+  RAYT_CUDA_TRY(launch_unique_from_bits(UniqueParams(it), s_));
+  *launches += 1 + (record ? 1 : 0);
+  RAYT_CUDA_TRY(cudaEventRecord(ev_[2], s_));
+  return RAYT_OK;
+}
+
 int Renderer::Frame(const float* m) {
   const auto t0 = std::chrono::steady_clock::now();
   stats = rayt_frame_stats{};
@@ -328,26 +470,7 @@ int Renderer::Frame(const float* m) {
   float ms_trace = 0, ms_fb = 0, ms_up = 0;
   int it;
   for (it = 0;; ++it) {
-    if ((rc = Prepare(it)) != RAYT_OK) break;
-    RAYT_CUDA_TRY(cudaEventRecord(ev_[0], s_));
-    if (it == 0 || active_prev > 0) {
-      if ((rc = Trace(it, false, active_prev)) != RAYT_OK) break;
-      launches += it == 0 ? groups() : 1;
-    }
-    RAYT_CUDA_TRY(cudaEventRecord(ev_[1], s_));
-    UniqueFromBitsParams q{};
-    q.fault_bits = reinterpret_cast<const uint32_t*>(d_state_ + kBlockInts);
-    q.fault_words = fault_words_;
-    q.hit_bits = reinterpret_cast<const uint32_t*>(d_state_ + kBlockInts + fault_words_);
-    q.hit_words = hit_words_;
-    q.n_words = block(it & 1);
-    q.n_rays = block(it & 1) + 1;
-    q.total_pixels = total;
-    q.unique_out = d_unique_;
-    q.counts_out = d_counts_;
-    RAYT_CUDA_TRY(launch_unique_from_bits(q, s_));
-    launches += 1 + (record ? 1 : 0);
-    RAYT_CUDA_TRY(cudaEventRecord(ev_[2], s_));
+    if ((rc = RunPass(it, active_prev, &launches)) != RAYT_OK) break;
     if (record) {
       if (!h_dense_) RAYT_CUDA_TRY(cudaHostAlloc(&h_dense_, (size_t)padded_pixels_ * 4, cudaHostAllocDefault));
       RAYT_CUDA_TRY(cudaMemcpyAsync(h_dense_, d_dense_, (size_t)padded_pixels_ * 4, cudaMemcpyDeviceToHost, s_));
@@ -474,6 +597,7 @@ int Renderer::Autotune(const float* m, int reps, int* best) {
   for (int t : kTiles)
     for (const Refill& r : kRefill)
       for (int c : kCtas) {
+        if (r.refill == 32 && c != 0) continue;  // CTAs per SM only shape the persistent kernel
         tile_w_log2 = t;
         refill = r.refill;
         step_budget = r.budget;
@@ -562,6 +686,11 @@ int rayt_renderer_set_max_passes(rayt_renderer* r, int n) {
 int rayt_renderer_seed(rayt_renderer* r, uint32_t seed) {
   if (!r) return fail(RAYT_E_ARG, "null renderer");
   R(r)->rand.Seed(seed);
+  return RAYT_OK;
+}
+int rayt_renderer_use_graphs(rayt_renderer* r, int on) {
+  if (!r) return fail(RAYT_E_ARG, "null renderer");
+  R(r)->use_graphs = on != 0;
   return RAYT_OK;
 }
 int rayt_renderer_record_passes(rayt_renderer* r, int on) {

@@ -660,6 +660,30 @@ __global__ void __launch_bounds__(kBlockThreads) trace_persistent_kernel(const _
   }
 }
 
+// Persistent form without lane refills, for the passes after the first: each
+// warp takes 32 rays at a time from the work counter and runs them to their
+// end.  Its grid does not depend on the ray count (read on the device), so the
+// pass can be replayed from a CUDA graph unchanged.
+template <bool kFirst, bool kCount>
+__global__ void __launch_bounds__(kBlockThreads) trace_queue_kernel(const __grid_constant__ TraceParams p) {
+  const int lane = threadIdx.x & 31;
+  const int total = kFirst ? p.total_tiles * 32 : *p.n_in;
+  for (;;) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(p.work, 32);
+    base = __shfl_sync(kFull, base, 0);
+    if (base >= total) break;
+    const int r = base + lane;
+    uint32_t ray;
+    float4 o, d;
+    if (r < total && ray_at<kFirst>(p, r, ray, o, d)) {
+      uint32_t fetches = 0, far_fetches = 0;
+      const RayEnd e = cast_ray<kCount>(p, o, d, fetches, far_fetches);
+      end_ray<kCount>(p, e, ray, o, d, fetches, far_fetches);
+    }
+  }
+}
+
 // FinishTracingFrame for rays still faulted at the end of the frame: shade
 // with the fault's parent node as the cache holds it now.
 __global__ void __launch_bounds__(kBlockThreads) finish_kernel(const __grid_constant__ TraceParams p) {
@@ -743,28 +767,40 @@ __global__ void __launch_bounds__(kUniqThreads) unique_from_bits_kernel(const Un
   }
 }
 
-template <bool kFirst, bool kCount>
-int persistent_grid() {
-  static int grid = 0;
-  if (!grid) {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_persistent_kernel<kFirst, kCount>, kBlockThreads, 0);
-    grid = sms * (per_sm > 0 ? per_sm : 1);
-  }
-  return grid;
+template <typename Kernel>
+int resident_grid(Kernel kernel) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlockThreads, 0);
+  return sms * (per_sm > 0 ? per_sm : 1);
 }
 
 template <bool kFirst, bool kCount>
-cudaError_t launch_variant(const TraceParams& p, int rays, int grid, cudaStream_t s) {
-  if (p.refill < 32) {
-    trace_persistent_kernel<kFirst, kCount><<<grid, kBlockThreads, 0, s>>>(p);
+int persistent_grid() {
+  static const int grid = resident_grid(trace_persistent_kernel<kFirst, kCount>);
+  return grid;
+}
+
+template <bool kCount>
+int queue_grid() {
+  static const int grid = resident_grid(trace_queue_kernel<false, kCount>);
+  return grid;
+}
+
+// The traversal launch for pass kind (first, count): function and grid.
+template <bool kFirst, bool kCount>
+void trace_launch_shape(const TraceParams& p, int rays, int grid, void** func, dim3* blocks) {
+  if (!kFirst) {
+    *func = reinterpret_cast<void*>(trace_queue_kernel<false, kCount>);
+    *blocks = dim3(queue_grid<kCount>());
+  } else if (p.refill < 32) {
+    *func = reinterpret_cast<void*>(trace_persistent_kernel<true, kCount>);
+    *blocks = dim3(grid > 0 ? grid : persistent_grid<true, kCount>());
   } else {
-    if (rays <= 0) return cudaSuccess;
-    trace_kernel<kFirst, kCount><<<(rays + kBlockThreads - 1) / kBlockThreads, kBlockThreads, 0, s>>>(p);
+    *func = reinterpret_cast<void*>(trace_kernel<true, kCount>);
+    *blocks = dim3((rays + kBlockThreads - 1) / kBlockThreads);
   }
-  return cudaGetLastError();
 }
 
 }  // namespace
@@ -774,9 +810,44 @@ int trace_persistent_grid(bool first, bool count) {
   return count ? persistent_grid<false, true>() : persistent_grid<false, false>();
 }
 
+cudaError_t trace_node_params(const TraceParams* p, bool first, bool count, int rays, int grid, void** args,
+                              cudaKernelNodeParams* kp) {
+  void* func = nullptr;
+  dim3 blocks;
+  if (first) {
+    if (count) trace_launch_shape<true, true>(*p, rays, grid, &func, &blocks);
+    else trace_launch_shape<true, false>(*p, rays, grid, &func, &blocks);
+  } else {
+    if (count) trace_launch_shape<false, true>(*p, rays, grid, &func, &blocks);
+    else trace_launch_shape<false, false>(*p, rays, grid, &func, &blocks);
+  }
+  args[0] = const_cast<TraceParams*>(p);
+  *kp = cudaKernelNodeParams{};
+  kp->func = func;
+  kp->gridDim = blocks;
+  kp->blockDim = dim3(kBlockThreads);
+  kp->sharedMemBytes = 0;
+  kp->kernelParams = args;
+  kp->extra = nullptr;
+  return cudaSuccess;
+}
+
 cudaError_t launch_trace(const TraceParams& p, bool first, bool count, int rays, int grid, cudaStream_t s) {
-  if (first) return count ? launch_variant<true, true>(p, rays, grid, s) : launch_variant<true, false>(p, rays, grid, s);
-  return count ? launch_variant<false, true>(p, rays, grid, s) : launch_variant<false, false>(p, rays, grid, s);
+  void* args[1];
+  cudaKernelNodeParams kp;
+  trace_node_params(&p, first, count, rays, grid, args, &kp);
+  if (kp.gridDim.x == 0) return cudaSuccess;
+  return cudaLaunchKernel(kp.func, kp.gridDim, kp.blockDim, kp.kernelParams, 0, s);
+}
+
+cudaError_t unique_node_params(const UniqueFromBitsParams* q, void** args, cudaKernelNodeParams* kp) {
+  args[0] = const_cast<UniqueFromBitsParams*>(q);
+  *kp = cudaKernelNodeParams{};
+  kp->func = reinterpret_cast<void*>(unique_from_bits_kernel);
+  kp->gridDim = dim3(1);
+  kp->blockDim = dim3(kUniqThreads);
+  kp->kernelParams = args;
+  return cudaSuccess;
 }
 
 cudaError_t launch_finish(const TraceParams& p, int max_rays, cudaStream_t s) {

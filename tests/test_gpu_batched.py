@@ -139,3 +139,25 @@ def test_batched_argument_errors(trees):
         rt.set_launch_shape(3, 0, 0)
     with pytest.raises(R.RaytError):
         rt.set_launch_shape(3, 16, 0, 0)
+
+
+def test_graphs_match_plain_launches(trees):
+    """Pass graphs (default) and plain launches give the same frames, including
+    after a launch-shape change that rebuilds the graphs."""
+    sizes = [(96, 64), (33, 17), (128, 72)]
+    frames = [[_matrix(c, w, h) for c, (w, h) in zip(_cams(len(sizes), 30.0 * f), sizes)] for f in range(6)]
+    runs = []
+    for graphs in (True, False):
+        ld, cm, rt = _gpu_views(trees["terrain8s"], 150, sizes, seed=23)
+        rt.use_graphs(graphs)
+        out = []
+        for f, mats in enumerate(frames):
+            if f == 3:
+                rt.set_launch_shape(3, 32, 0, 16)
+            rt.RenderViews(mats)
+            out.append((rt.stats()["passes"], [rt.read_image(view=v).copy() for v in range(len(sizes))]))
+        runs.append(out)
+    for f, (a, b) in enumerate(zip(*runs)):
+        assert a[0] == b[0], "frame %d" % f
+        for v in range(len(sizes)):
+            np.testing.assert_array_equal(a[1][v], b[1][v], err_msg="frame %d view %d" % (f, v))
