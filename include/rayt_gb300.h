@@ -257,6 +257,62 @@ int rayt_renderer_count_fetches(rayt_renderer* r, const float* view_proj_inv, in
 int rayt_renderer_time_pass(rayt_renderer* r, const float* view_proj_inv, int reps, float* ms_per_pass);
 
 /* ------------------------------------------------------------------------ */
+/* Served form (no counterpart in the reference).  Frame requests of up to 64
+ * clients against one shared cache, with continuous batching: every
+ * scheduling tick is one pass over all requests in flight (new requests'
+ * first passes and older requests' faulted rays in the same launches), one
+ * feedback unique and one cache transaction.  Clients are admitted while
+ * framebuffer memory is free; requests while ray-record capacity is free, one
+ * per client at a time, in arrival order.  Faulted rays restart from the
+ * camera, so a request that ends without hitting its pass cap has exactly the
+ * image of a fully resident cache, whatever else shared its ticks. */
+
+typedef struct rayt_server rayt_server;
+typedef struct {
+  int max_clients;             /* 1..64 */
+  int64_t framebuffer_bytes;   /* device memory for all client framebuffers */
+  int64_t max_rays_in_flight;  /* ray records held between passes (request admission) */
+  int max_passes;              /* tracing passes per request before its faulted rays are shaded */
+  float lod_voxel_size;
+  int deliver_to_host;         /* copy every finished frame to the client's pinned host image */
+} rayt_server_config;
+typedef struct {
+  uint64_t request;
+  int client;
+  int passes;                  /* tracing passes the request took */
+  int truncated;               /* 1: rays still faulting at the end were shaded with their fault parent */
+  double submit_s, admit_s, done_s;  /* steady-clock seconds */
+} rayt_request_info;
+typedef struct {
+  int64_t submitted, completed, ticks, rays_traced, faults, kernel_launches, bytes_d2h;
+} rayt_server_stats;
+
+int rayt_server_create(rayt_cache* cache, const rayt_server_config* cfg, rayt_server** out);
+void rayt_server_destroy(rayt_server* s);
+/* RAYT_E_LIMIT when no slot or framebuffer memory is free.  Add and remove
+ * clients while the scheduler thread is stopped. */
+int rayt_server_add_client(rayt_server* s, int width, int height, int* client);
+int rayt_server_remove_client(rayt_server* s, int client);
+int rayt_server_seed(rayt_server* s, uint32_t seed);
+/* Queues a frame of `client` (thread-safe). */
+int rayt_server_submit(rayt_server* s, int client, const float view_proj_inv[16], uint64_t* request);
+/* One scheduling tick on the calling thread; *finished = requests it ended. */
+int rayt_server_step(rayt_server* s, int* finished);
+/* Scheduler thread running ticks while requests are queued or in flight. */
+int rayt_server_start(rayt_server* s);
+int rayt_server_stop(rayt_server* s);
+/* Blocks until `request` ended (running ticks itself when no scheduler thread
+ * runs); each request's info is returned once. */
+int rayt_server_wait(rayt_server* s, uint64_t request, double timeout_s, rayt_request_info* out);
+/* The client's framebuffer: its last finished frame until its next request
+ * is admitted. */
+int rayt_server_client_image(rayt_server* s, int client, void** device_rgba);
+int rayt_server_read_client_image(rayt_server* s, int client, void* host_rgba, size_t bytes);
+/* With deliver_to_host: the pinned host copy of the client's last finished frame. */
+int rayt_server_host_image(rayt_server* s, int client, const void** host_rgba);
+int rayt_server_stats_get(const rayt_server* s, rayt_server_stats* out);
+
+/* ------------------------------------------------------------------------ */
 /* Feedback primitives on device arrays of int32. */
 
 /* GPUSort::Sort (rayt/GPU algorithms/gpu-sort.cpp:16-49): ascending signed

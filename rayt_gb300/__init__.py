@@ -67,6 +67,21 @@ class FrameStats(C.Structure):
                 ("bytes_h2d", C.c_int64), ("bytes_d2h", C.c_int64)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("max_clients", C.c_int), ("framebuffer_bytes", C.c_int64), ("max_rays_in_flight", C.c_int64),
+                ("max_passes", C.c_int), ("lod_voxel_size", C.c_float), ("deliver_to_host", C.c_int)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("request", C.c_uint64), ("client", C.c_int), ("passes", C.c_int), ("truncated", C.c_int),
+                ("submit_s", C.c_double), ("admit_s", C.c_double), ("done_s", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(k, C.c_int64) for k in ["submitted", "completed", "ticks", "rays_traced", "faults",
+                                         "kernel_launches", "bytes_d2h"]]
+
+
 class CameraStruct(C.Structure):
     _fields_ = [("yaw", C.c_float), ("pitch", C.c_float), ("roll", C.c_float), ("position", C.c_float * 3),
                 ("field_of_view", C.c_float), ("aspect_ratio", C.c_float), ("near_clip_plane", C.c_float)]
@@ -136,6 +151,20 @@ def lib():
         "rayt_renderer_set_launch_shape": (i32, [vp, i32, i32, i32, i32]),
         "rayt_renderer_get_launch_shape": (i32, [vp, C.POINTER(i32)]),
         "rayt_renderer_autotune": (i32, [vp, C.POINTER(f32), i32, C.POINTER(i32)]),
+        "rayt_server_create": (i32, [vp, C.POINTER(ServerConfig), C.POINTER(vp)]),
+        "rayt_server_destroy": (None, [vp]),
+        "rayt_server_add_client": (i32, [vp, i32, i32, C.POINTER(i32)]),
+        "rayt_server_remove_client": (i32, [vp, i32]),
+        "rayt_server_seed": (i32, [vp, u32]),
+        "rayt_server_submit": (i32, [vp, i32, C.POINTER(f32), C.POINTER(C.c_uint64)]),
+        "rayt_server_step": (i32, [vp, C.POINTER(i32)]),
+        "rayt_server_start": (i32, [vp]),
+        "rayt_server_stop": (i32, [vp]),
+        "rayt_server_wait": (i32, [vp, C.c_uint64, C.c_double, C.POINTER(RequestInfo)]),
+        "rayt_server_client_image": (i32, [vp, i32, C.POINTER(vp)]),
+        "rayt_server_read_client_image": (i32, [vp, i32, vp, C.c_size_t]),
+        "rayt_server_host_image": (i32, [vp, i32, C.POINTER(vp)]),
+        "rayt_server_stats_get": (i32, [vp, C.POINTER(ServerStats)]),
         "rayt_sort_i32": (i32, [vp, i32, vp]),
         "rayt_scan_i32": (i32, [vp, i32, vp]),
         "rayt_feedback_unique": (i32, [vp, i32, i32, vp, C.POINTER(i32), vp]),
@@ -441,6 +470,88 @@ class GPURayTracer:
     def close(self):
         if self._h:
             lib().rayt_renderer_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class RenderServer:
+    """Served form: frames of many clients against one shared cache with
+    continuous batching (rayt_server_*).  No counterpart in the reference."""
+
+    def __init__(self, cache_manager, max_clients=16, framebuffer_bytes=1 << 30, max_rays_in_flight=1 << 25,
+                 max_passes=8, lod_voxel_size=1.0, deliver_to_host=False):
+        self.cache = cache_manager
+        cfg = ServerConfig(max_clients, framebuffer_bytes, max_rays_in_flight, max_passes, lod_voxel_size,
+                           1 if deliver_to_host else 0)
+        h = C.c_void_p()
+        _check(lib().rayt_server_create(cache_manager.handle, C.byref(cfg), C.byref(h)))
+        self._h = h
+        self.sizes = {}
+
+    def add_client(self, width, height):
+        c = C.c_int()
+        _check(lib().rayt_server_add_client(self._h, width, height, C.byref(c)))
+        self.sizes[c.value] = (width, height)
+        return c.value
+
+    def remove_client(self, client):
+        _check(lib().rayt_server_remove_client(self._h, client))
+        self.sizes.pop(client, None)
+
+    def seed(self, seed):
+        _check(lib().rayt_server_seed(self._h, seed))
+
+    def submit(self, client, camera_or_matrix):
+        if isinstance(camera_or_matrix, Camera):
+            camera_or_matrix = camera_or_matrix.view_proj_inv()
+        m, p = _mat(camera_or_matrix)
+        r = C.c_uint64()
+        _check(lib().rayt_server_submit(self._h, client, p, C.byref(r)))
+        return r.value
+
+    def step(self):
+        n = C.c_int()
+        _check(lib().rayt_server_step(self._h, C.byref(n)))
+        return n.value
+
+    def start(self):
+        _check(lib().rayt_server_start(self._h))
+
+    def stop(self):
+        _check(lib().rayt_server_stop(self._h))
+
+    def wait(self, request, timeout=60.0):
+        info = RequestInfo()
+        _check(lib().rayt_server_wait(self._h, request, timeout, C.byref(info)))
+        return {k: getattr(info, k) for k, _ in RequestInfo._fields_}
+
+    def read_image(self, client, out=None):
+        w, h = self.sizes[client]
+        if out is None:
+            out = np.zeros((h, w, 4), np.uint8)
+        _check(lib().rayt_server_read_client_image(self._h, client, out.ctypes.data, out.nbytes))
+        return out
+
+    def host_image(self, client):
+        """Zero-copy view of the pinned host copy of the client's last frame."""
+        w, h = self.sizes[client]
+        p = C.c_void_p()
+        _check(lib().rayt_server_host_image(self._h, client, C.byref(p)))
+        return np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_uint8)), shape=(h, w, 4))
+
+    def stats(self):
+        s = ServerStats()
+        _check(lib().rayt_server_stats_get(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in ServerStats._fields_}
+
+    def close(self):
+        if self._h:
+            lib().rayt_server_destroy(self._h)
             self._h = None
 
     def __del__(self):

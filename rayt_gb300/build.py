@@ -20,7 +20,7 @@ CU_FLAGS = ["-O3", "-std=c++17", "--fmad=false", "-prec-div=true", "-prec-sqrt=t
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-pthread"]
 
 CU_SOURCES = ["trace.cu", "sort.cu", "upload.cu", "unique_noalloc.cu"]
-CXX_SOURCES = ["util.cpp", "tree.cpp", "cache.cpp", "renderer.cpp", "prims.cpp"]
+CXX_SOURCES = ["util.cpp", "tree.cpp", "cache.cpp", "renderer.cpp", "server.cpp", "prims.cpp"]
 
 
 def _run(cmd):

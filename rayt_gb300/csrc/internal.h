@@ -27,6 +27,7 @@ constexpr uint32_t kRootParent = (1u << 24) - 1;
 // index in that buffer, below 2^30.
 constexpr int kMaxViews = 512;
 constexpr int kViewsPerLaunch = 64;   // view descriptors travel in the launch parameters
+constexpr int kMaxClients = 64;       // served mode: client framebuffers per server
 
 // One view of a tracing launch.
 struct ViewDesc {
@@ -74,11 +75,26 @@ struct TraceParams {
   uint32_t* hit_bits;      // bit 2*cache_block + dup
   int* n_words;            // number of non-NO_HIT words this pass
   unsigned long long* counters;  // optional: rays, link fetches, far fetches, iterations, hits, faults
-  // persistent kernel only
+  // served mode (zero in the per-frame path).  Client slot i owns the pixels
+  // [client_base[i], client_base[i + 1]) of the image buffer.
+  int restart;             // faulted rays are recorded with their camera origin and traced afresh
+  int n_clients;
+  int client_base[kMaxClients + 1];
+  unsigned long long finish_mask;  // continuation rays of these slots are finished, not traced
+  int* client_faults;      // per slot: rays that faulted in this pass
+  // persistent kernels
   int* work;               // work counter, zero before the launch
   int refill;              // idle lanes that let a warp take new rays (< 32)
   int step_budget;         // iterations a warp runs between refill checks
   ViewDesc views[kViewsPerLaunch];
+};
+
+// Faulted-ray records carried from one pass to the next (device arrays).
+struct RayList {
+  float4* origin = nullptr;  // xyz advanced to the fault, w LOD bias
+  float4* dir = nullptr;     // xyz direction, w LOD coefficient
+  int* parent = nullptr;     // node the ray faulted under
+  uint32_t* ray = nullptr;   // pixel index in the image buffer
 };
 
 // first: rays come from the views' cameras (refill = 32: one thread per ray

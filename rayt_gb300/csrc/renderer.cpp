@@ -21,17 +21,10 @@
 #include <memory>
 
 #include "cache.h"
+#include "feedback.h"
 #include "internal.h"
 
 namespace rayt {
-
-// Faulted-ray records carried from one pass to the next.
-struct RayList {
-  float4* origin = nullptr;  // xyz advanced to the fault, w LOD bias
-  float4* dir = nullptr;     // xyz direction, w LOD coefficient
-  int* parent = nullptr;     // node the ray faulted under
-  uint32_t* ray = nullptr;   // view << kRayPixelBits | pixel
-};
 
 class Renderer {
  public:
@@ -65,8 +58,6 @@ class Renderer {
   static constexpr int kBlockInts = 16;  // pass block: {words, rays out, pad, pad, work counter per launch group}
   Cache* cache_ = nullptr;
   int total_pixels_ = 0, padded_pixels_ = 0;
-  int expected_faults_ = 1 << 16;  // ray-tracing-feedback-extractor.cpp:22-23
-  int hits_to_extract_ = 4000;
   cudaStream_t s_ = nullptr;
   std::vector<ViewDesc> views_;     // sizes, tile layout and matrices of the current frame
   std::vector<int> group_tiles_;    // first-pass tiles per launch group of kViewsPerLaunch views
@@ -87,13 +78,12 @@ class Renderer {
   uint8_t* d_flush_ = nullptr;       // L2 flush buffer for TimePass
   cudaEvent_t ev_[8] = {};
   std::vector<std::vector<int32_t>> pass_words_;
-  std::vector<int> faults_, hits_, dup_hits_;
+  FeedbackDecoder fb_;
 
   int* block(int k) const { return k ? d_state_ + kBlockInts + fault_words_ + hit_words_ : d_state_; }
   int SetViews(const float* m);
   TraceParams Params(int it) const;
   int Grid(bool first, bool count) const;
-  void Decode(int count);
   int Prepare(int it);
   int Trace(int it, bool count, int rays);
   UniqueFromBitsParams UniqueParams(int it) const;
@@ -267,48 +257,6 @@ int Renderer::Grid(bool first, bool count) const {
   return std::min(full, sms * ctas_per_sm);
 }
 
-// ProcessUnique + AdjustExpectedFaults (ray-tracing-feedback-extractor.cpp:108-185)
-// over the unique array in mapped host memory.
-void Renderer::Decode(int count) {
-  faults_.clear();
-  hits_.clear();
-  dup_hits_.clear();
-  const int32_t* u = h_unique_;
-  auto add_hit = [this](int32_t v) {
-    if (v & 1) dup_hits_.push_back((v >> 1) - 1);
-    else hits_.push_back((v >> 1) - 1);
-  };
-  int stride = expected_faults_, size = 0;
-  while (size < count && (size == 0 || u[size - 1] < 0)) {
-    stride = std::min(stride, count - size);
-    for (int i = size; i < size + stride; ++i) {
-      if (u[i] < 0) faults_.push_back(-u[i] - 1);
-      else if (u[i] != kNoHit) add_hit(u[i]);
-    }
-    size += stride;
-    stride *= 2;
-  }
-  if (size < count) {
-    const int len = count - size;
-    const int start = rand.Next() % len;
-    const int take = std::min(hits_to_extract_, len);
-    int seg[2][2];
-    int nseg = 0;
-    if (start + take <= len) {
-      seg[nseg][0] = start; seg[nseg][1] = take; ++nseg;
-    } else {
-      seg[nseg][0] = 0; seg[nseg][1] = start + take - len; ++nseg;
-      seg[nseg][0] = start; seg[nseg][1] = len - start; ++nseg;
-    }
-    for (int k = 0; k < nseg; ++k)
-      for (int i = 0; i < seg[k][1]; ++i) {
-        const int32_t v = u[size + seg[k][0] + i];
-        if (v != kNoHit) add_hit(v);
-      }
-  }
-  if (expected_faults_ > 1 && (int)faults_.size() < expected_faults_) expected_faults_ /= 2;
-  else if ((int)faults_.size() > expected_faults_) expected_faults_ *= 2;
-}
 
 // Clears pass `it`'s block and the feedback bitmaps (one contiguous range).
 int Renderer::Prepare(int it) {
@@ -497,22 +445,22 @@ int Renderer::Frame(const float* m) {
     if (it > 0 && el > time_limit) { active_prev = active_now; break; }
     if (max_passes > 0 && it > 0 && it + 1 >= max_passes) { active_prev = active_now; break; }
 
-    Decode(h_counts_[0]);
+    fb_.Decode(h_unique_, h_counts_[0], rand);
     if ((rc = cache_->StartTransaction()) != RAYT_OK) break;
-    for (int b2 : hits_) cache_->MarkBlockUsed(b2);
-    for (int b2 : dup_hits_) cache_->MarkParentUsed(b2);
-    for (int f : faults_) {
+    for (int b2 : fb_.hits) cache_->MarkBlockUsed(b2);
+    for (int b2 : fb_.dup_hits) cache_->MarkParentUsed(b2);
+    for (int f : fb_.faults) {
       if (cache_->TransactionFilled()) break;
       if ((rc = cache_->RequestBlock(f)) != RAYT_OK) break;
     }
-    stats.faults += (int)faults_.size();
+    stats.faults += (int)fb_.faults.size();
     RAYT_CUDA_TRY(cudaEventRecord(ev_[3], s_));
     const int erc = cache_->EndTransaction();
     RAYT_CUDA_TRY(cudaEventRecord(ev_[4], s_));
     if (rc == RAYT_OK) rc = erc;
     if (rc != RAYT_OK) break;
     active_prev = active_now;
-    if (faults_.empty() || cache_->SessionFilled()) break;
+    if (fb_.faults.empty() || cache_->SessionFilled()) break;
   }
   stats.passes = it + 1;
   stats.session_filled = cache_->in_session() && cache_->SessionFilled() ? 1 : 0;

@@ -497,6 +497,17 @@ __device__ __forceinline__ int view_of_tile(const TraceParams& p, int tile) {
   return lo;
 }
 
+// Served mode: the client slot owning pixel `ray` (client_base ascending).
+__device__ __forceinline__ int slot_of(const TraceParams& p, uint32_t ray) {
+  int lo = 0, hi = p.n_clients - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if ((uint32_t)p.client_base[mid] <= ray) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
 // Pixel (x, y) and view of first-pass ray r (tile r / 32, lane r % 32);
 // false for the lanes of a partial tile that fall outside the view.
 __device__ __forceinline__ bool first_pass_pixel(const TraceParams& p, int r, int& v, int& x, int& y) {
@@ -556,11 +567,14 @@ __device__ __forceinline__ void end_ray(const TraceParams& p, const RayEnd& e, u
   }
   if (p.words_dense) p.words_dense[ray] = word;
   const int slot = warp_append(p.n_out, faulted);
-  if (faulted) {  // origin moved to the fault
-    o.x = o.x + d.x * e.t;
-    o.y = o.y + d.y * e.t;
-    o.z = o.z + d.z * e.t;
-    o.w = o.w + d.w * e.t;
+  if (faulted) {
+    if (!p.restart) {  // origin moved to the fault (raytracing_pass.cl:37-41)
+      o.x = o.x + d.x * e.t;
+      o.y = o.y + d.y * e.t;
+      o.z = o.z + d.z * e.t;
+      o.w = o.w + d.w * e.t;
+    }
+    if (p.client_faults) atomicAdd(p.client_faults + slot_of(p, ray), 1);
     p.out_origin[slot] = o;
     p.out_dir[slot] = d;
     p.out_parent[slot] = node;
@@ -677,9 +691,16 @@ __global__ void __launch_bounds__(kBlockThreads) trace_queue_kernel(const __grid
     uint32_t ray;
     float4 o, d;
     if (r < total && ray_at<kFirst>(p, r, ray, o, d)) {
-      uint32_t fetches = 0, far_fetches = 0;
-      const RayEnd e = cast_ray<kCount>(p, o, d, fetches, far_fetches);
-      end_ray<kCount>(p, e, ray, o, d, fetches, far_fetches);
+      if (!kFirst && p.finish_mask && ((p.finish_mask >> slot_of(p, ray)) & 1ull)) {
+        // served mode: the request stops here; FinishTracingFrame's shading
+        // with the fault's parent node
+        const uchar4 col = (p.normals && p.colors) ? shade(p, p.in_parent[r]) : make_uchar4(0, 0, 0, 0);
+        p.image[ray] = finish(p, col);
+      } else {
+        uint32_t fetches = 0, far_fetches = 0;
+        const RayEnd e = cast_ray<kCount>(p, o, d, fetches, far_fetches);
+        end_ray<kCount>(p, e, ray, o, d, fetches, far_fetches);
+      }
     }
   }
 }

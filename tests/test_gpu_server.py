@@ -1,0 +1,143 @@
+"""GPU tests of the served form (rayt_server_*): continuous batching of many
+clients' frames against one shared, streamed cache.  Faulted rays restart
+from the camera, so every request that ends without truncation must equal the
+one-view oracle frame of its camera over a fully resident cache, alone or in
+any mix."""
+import threading
+
+import numpy as np
+import pytest
+
+import rayt_gb300 as R
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [(96, 64), (160, 90), (33, 17), (128, 128), (64, 48)]
+
+
+def _cam(a, v=0):
+    return [a, -20.0 - 5 * (v % 3), 0.0, 0.5 - 0.6 * np.sin(np.radians(a)), 0.72,
+            0.5 + 0.6 * np.cos(np.radians(a)), 60.0]
+
+
+def _matrix(cam, w, h):
+    return R.Camera(cam[0], cam[1], cam[2], cam[3:6], cam[6], w / h).view_proj_inv()
+
+
+_REF = {}
+
+
+def _resident(trees, w, h, m):
+    """The oracle's one-view frame over the whole tree in the cache."""
+    from oracle import oracle as O
+    key = (w, h, np.asarray(m, np.float32).tobytes())
+    if key not in _REF:
+        sc = O.OracleScene(trees["terrain8s"], 0, w, h)
+        _, img = sc.render(m)
+        sc.close()
+        _REF[key] = img
+    return _REF[key]
+
+
+def _server(trees, max_blocks=640, **kw):
+    ld = R.StoredOctreeLoader(trees["terrain8s"])
+    cm = R.GPUOctreeCacheManager(max_blocks, ld)
+    cm.InitialFillCache()
+    args = dict(max_clients=8, framebuffer_bytes=16 << 20, max_rays_in_flight=1 << 20, max_passes=32)
+    args.update(kw)
+    return ld, cm, R.RenderServer(cm, **args)
+
+
+def test_served_alone_and_mixed_equal_resident_oracle(trees):
+    frames = 4
+    mats = {v: [_matrix(_cam(40.0 * f + 70 * v, v), w, h) for f in range(frames)] for v, (w, h) in enumerate(SIZES)}
+    # alone: one client at a time
+    alone = {}
+    for v, (w, h) in enumerate(SIZES):
+        ld, cm, srv = _server(trees)
+        c = srv.add_client(w, h)
+        for f in range(frames):
+            info = srv.wait(srv.submit(c, mats[v][f]))
+            assert not info["truncated"]
+            alone[v, f] = srv.read_image(c)
+        srv.close()
+    # mixed: all clients submit together; frames of different clients share ticks
+    ld, cm, srv = _server(trees)
+    ids = [srv.add_client(w, h) for w, h in SIZES]
+    for f in range(frames):
+        reqs = [srv.submit(ids[v], mats[v][f]) for v in range(len(SIZES))]
+        for v, r in enumerate(reqs):
+            info = srv.wait(r)
+            assert not info["truncated"] and info["client"] == ids[v]
+            img = srv.read_image(ids[v])
+            np.testing.assert_array_equal(img, alone[v, f], err_msg="client %d frame %d" % (v, f))
+            w, h = SIZES[v]
+            np.testing.assert_array_equal(img, _resident(trees, w, h, mats[v][f]), err_msg="oracle %d %d" % (v, f))
+    st = srv.stats()
+    assert st["completed"] == frames * len(SIZES)
+    assert st["faults"] > 0  # blocks were streamed while the frames shared ticks
+    assert st["ticks"] < frames * sum(1 for _ in SIZES) * 3  # frames shared ticks
+
+
+def test_served_scheduler_thread_and_concurrent_submitters(trees):
+    ld, cm, srv = _server(trees, deliver_to_host=True)
+    ids = [srv.add_client(w, h) for w, h in SIZES]
+    srv.start()
+    results = {}
+
+    def client(v):
+        w, h = SIZES[v]
+        for f in range(3):
+            m = _matrix(_cam(33.0 * f + 50 * v, v), w, h)
+            info = srv.wait(srv.submit(ids[v], m), timeout=120)
+            results[v, f] = (info, srv.host_image(ids[v]).copy(), m)
+
+    threads = [threading.Thread(target=client, args=(v,)) for v in range(len(SIZES))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    srv.stop()
+    assert len(results) == 3 * len(SIZES)
+    for (v, f), (info, img, m) in results.items():
+        assert info["done_s"] >= info["admit_s"] >= info["submit_s"]
+        if not info["truncated"]:
+            w, h = SIZES[v]
+            np.testing.assert_array_equal(img, _resident(trees, w, h, m), err_msg="client %d frame %d" % (v, f))
+
+
+def test_served_admission_limits(trees):
+    # framebuffer memory admits clients: 2 frames of 128x128 fit, a third does not
+    ld, cm, srv = _server(trees, framebuffer_bytes=2 * 128 * 128 * 4)
+    a = srv.add_client(128, 128)
+    b = srv.add_client(128, 128)
+    with pytest.raises(R.RaytError):
+        srv.add_client(128, 128)
+    srv.remove_client(b)
+    c = srv.add_client(64, 64)
+    # ray-record capacity admits requests: one 128x128 request at a time
+    srv.close()
+    ld, cm, srv = _server(trees, max_rays_in_flight=128 * 128)
+    a = srv.add_client(128, 128)
+    b = srv.add_client(128, 128)
+    ra = srv.submit(a, _matrix(_cam(10.0), 128, 128))
+    rb = srv.submit(b, _matrix(_cam(100.0), 128, 128))
+    ia, ib = srv.wait(ra), srv.wait(rb)
+    assert ib["admit_s"] >= ia["done_s"] - 1e-3  # b waited for a's records
+    # one request per client at a time, in order
+    r1 = srv.submit(a, _matrix(_cam(20.0), 128, 128))
+    r2 = srv.submit(a, _matrix(_cam(30.0), 128, 128))
+    i2 = srv.wait(r2)
+    i1 = srv.wait(r1)
+    assert i2["admit_s"] >= i1["done_s"] - 1e-3
+    np.testing.assert_array_equal(srv.read_image(a), _resident(trees, 128, 128, _matrix(_cam(30.0), 128, 128)))
+
+
+def test_served_pass_cap_truncates(trees):
+    ld, cm, srv = _server(trees, max_blocks=60, max_passes=1)
+    c = srv.add_client(160, 90)
+    info = srv.wait(srv.submit(c, _matrix(_cam(0.0), 160, 90)))
+    assert info["passes"] == 1
+    assert info["truncated"] == 1
+    img = srv.read_image(c)
+    assert img[..., 3].min() == 255  # every pixel was written
