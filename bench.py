@@ -1,6 +1,6 @@
 """Benchmark of the per-frame path on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload c3|c1|c2|c4]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload c3|c1|c2|c4|c5]
 
 The default workload is c3, the configuration the Mrays/s-at-1080p metric is
 quoted on.
@@ -18,6 +18,11 @@ builder; no public dataset is involved):
   c4  the c3 scene, 64 views per frame of sizes drawn from {256^2, 640x480,
       1280x720, 1920x1080} (seed 7), view v on its own spline (seed 7 + v),
       through the batched renderer; the plain per-view path is timed beside it
+  c5  depth-14 heightfield + spheres (16384^3), 16 clients of sizes drawn from
+      {1280x720, 1920x1080, 2560x1440} (seed 100), client c on its own spline
+      (seed 100 + c), frame requests Poisson at 60 Hz per client (seed 11),
+      through the server (continuous batching, 40 GB shared cache) and through
+      the plain per-frame path on the same schedule
 
 --impl reference times the reference algorithm's CPU implementation (the
 oracle restatement in oracle/, all host threads) on the same workload.
@@ -49,6 +54,14 @@ WORKLOADS = {
     # frame measures batched traversal + feedback rather than streaming
     "c4": {"depth": 12, "spheres": 2000, "width": 0, "height": 0, "cache_bytes": 0, "lod": 1.0, "views": 64,
            "sizes": [(256, 256), (640, 480), (1280, 720), (1920, 1080)], "size_seed": 7},
+    # 16 clients, Poisson 60 Hz each, against one shared cache of up to 40 GB.
+    # The cache format's 21-bit far-pointer slots address fewer than 2^18
+    # blocks, so the scene uses 8192-node blocks: the cache then holds up to
+    # 25.8 GB, which is more than the whole tree (about 16 GB)
+    "c5": {"depth": 14, "spheres": 2000, "width": 0, "height": 0, "cache_bytes": 40 << 30, "nib": 8192,
+           "lod": 1.0,
+           "clients": 16, "sizes": [(1280, 720), (1920, 1080), (2560, 1440)], "size_seed": 100,
+           "rate_hz": 60.0, "arrival_seed": 11, "seconds": 2.0, "closed_frames": 20, "max_passes": 8},
 }
 
 
@@ -58,16 +71,19 @@ def parse():
     ap.add_argument("--steps", type=int, default=0)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4"])
+    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4", "c5"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU baseline sample")
     ap.add_argument("--spheres", type=int, default=None, help="override the workload's sphere count")
     ap.add_argument("--cache-mib", type=int, default=None, help="override the workload's cache size")
+    ap.add_argument("--depth", type=int, default=None, help="override the workload's octree depth")
     a = ap.parse_args()
     if a.workload in WORKLOADS:
         if a.spheres is not None:
             WORKLOADS[a.workload]["spheres"] = a.spheres
         if a.cache_mib is not None:
             WORKLOADS[a.workload]["cache_bytes"] = a.cache_mib << 20
+        if a.depth is not None:
+            WORKLOADS[a.workload]["depth"] = a.depth
     return a
 
 
@@ -188,12 +204,13 @@ def profile_traffic(name):
 def scene_path(wl, local_rank, world):
     cfg = WORKLOADS[wl]
     os.makedirs(SCENE_DIR, exist_ok=True)
-    path = os.path.join(SCENE_DIR, "terrain_d%d_s%d_n4096.tree" % (cfg["depth"], cfg["spheres"]))
+    nib = cfg.get("nib", 4096)
+    path = os.path.join(SCENE_DIR, "terrain_d%d_s%d_n%d.tree" % (cfg["depth"], cfg["spheres"], nib))
     done = path + ".ok"
     if local_rank == 0 and not os.path.exists(done):
         import rayt_gb300 as R
         t = time.time()
-        R.build_terrain(path + ".tmp", cfg["depth"], 4096, spheres=cfg["spheres"], min_radius=8, max_radius=256)
+        R.build_terrain(path + ".tmp", cfg["depth"], nib, spheres=cfg["spheres"], min_radius=8, max_radius=256)
         os.replace(path + ".tmp", path)
         open(done, "w").write("%.1f\n" % (time.time() - t))
     barrier(world)
@@ -236,9 +253,11 @@ def camera_path(wl, frames, w, h, seed=3):
 
 
 def cache_blocks(cfg):
+    """Cache blocks for the workload's cache bytes (12 bytes a node), at most
+    2^18 - 1 (the cache format's far-pointer slots); 0 = the whole tree."""
     if not cfg["cache_bytes"]:
         return 0
-    return int(cfg["cache_bytes"] // (4096 * 12))
+    return int(min(cfg["cache_bytes"] // (cfg.get("nib", 4096) * 12), (1 << 18) - 1))
 
 
 # ---------------------------------------------------------------------------
@@ -548,6 +567,262 @@ def bench_batched(args, rank, world, local):
         "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clk}
 
 
+def served_schedule(cfg):
+    """C5: client sizes, per-client cameras and the merged Poisson arrival
+    schedule [(t, client, frame index)] over cfg["seconds"]."""
+    rng = np.random.default_rng(cfg["size_seed"])
+    pick = rng.integers(0, len(cfg["sizes"]), size=cfg["clients"])
+    sizes = [tuple(cfg["sizes"][k]) for k in pick]
+    arr = np.random.default_rng(cfg["arrival_seed"])
+    sched = []
+    for c in range(cfg["clients"]):
+        t, f = 0.0, 0
+        while True:
+            t += arr.exponential(1.0 / cfg["rate_hz"])
+            if t >= cfg["seconds"]:
+                break
+            sched.append((t, c, f))
+            f += 1
+    sched.sort()
+    return sizes, sched
+
+
+def _pcts(lat_ms):
+    a = np.sort(np.asarray(lat_ms, dtype=np.float64))
+    return round(float(np.percentile(a, 50)), 3), round(float(np.percentile(a, 99)), 3)
+
+
+def bench_served(args, rank, world, local):
+    """C5: the served form (RenderServer: scheduler thread, continuous
+    batching, shared cache) against the plain per-frame path (one
+    GPURayTracer per client, RenderFrame per request in arrival order), on the
+    same Poisson schedule (open loop: latency) and with every client keeping
+    one frame outstanding (closed loop: throughput).  Every phase has a wall
+    clock cap; progress goes to stderr."""
+    import threading
+
+    import torch
+
+    import rayt_gb300 as R
+    wl = "c5"
+    cfg = WORKLOADS[wl]
+    closed_frames = args.steps or cfg["closed_frames"]
+    path = scene_path(wl, local, world)
+    sizes, sched = served_schedule(cfg)
+    nclients = cfg["clients"]
+    frames_per_client = [1 + max([f for (_, c, f) in sched if c == cc] + [0]) for cc in range(nclients)]
+    nframes = max(frames_per_client + [closed_frames + args.warmup]) + 1
+    cams = [camera_path("c3", nframes, w, h, seed=cfg["size_seed"] + c) for c, (w, h) in enumerate(sizes)]
+    pixels = [w * h for w, h in sizes]
+    metric = "frames/s at 16 clients (served, continuous batching), depth 14"
+    threads = os.cpu_count() or 1
+    t_begin = time.time()
+
+    def log(msg):
+        sys.stderr.write("[c5 %7.1fs] %s\n" % (time.time() - t_begin, msg))
+        sys.stderr.flush()
+
+    def cpu_sample(budget):
+        """The oracle on the schedule's requests of one client size, one after
+        another, with a 32768-block cache (it streams like the reference)."""
+        from oracle import oracle as O
+        w, h = sizes[0]
+        sc = O.OracleScene(path, 32768, w, h, cfg["lod"])
+        el, k = 0.0, 0
+        for (t, c, f) in sched:
+            if sizes[c] != (w, h):
+                continue
+            tt = time.time()
+            sc.render(cams[c][f])
+            el += time.time() - tt
+            k += 1
+            if el > budget:
+                break
+        sc.close()
+        return k, el
+
+    if args.impl == "reference":
+        if rank != 0:
+            return None
+        k, el = cpu_sample(args.cpu_seconds * 3)
+        v = k / el
+        return {"metric": metric, "value": round(v, 3), "unit": "frames/s", "impl": "reference", "n_gpus": 1,
+                "steps": k, "warmup": 0, "ms_per_step": round(el / k * 1e3, 3), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": wl, "clients": nclients, "depth": cfg["depth"]},
+                "cpu_baseline": {"value": round(v, 3), "unit": "frames/s", "cores": threads, "kind": "port",
+                                 "sample": "%d %dx%d requests of the schedule (oracle, OpenMP)" % ((k,) + sizes[0])},
+                "e2e": {"value": round(v, 3), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+    torch.cuda.set_device(local)
+    log("scene ready")
+    ld = R.StoredOctreeLoader(path)
+    cm = R.GPUOctreeCacheManager(cache_blocks(cfg), ld)
+    t0 = time.time()
+    cm.InitialFillCache()
+    fill_s = time.time() - t0
+    loaded, cap_blocks = cm.blocks()
+    log("initial fill %.1fs: %d of %d tree blocks in a %d-block cache" % (fill_s, loaded, ld.info.blocks_count,
+                                                                          cap_blocks))
+    fb_bytes = sum(((p + 63) // 64) * 64 * 4 for p in pixels) + (1 << 20)
+
+    def make_server(deliver):
+        srv = R.RenderServer(cm, max_clients=nclients, framebuffer_bytes=fb_bytes, max_rays_in_flight=sum(pixels),
+                             max_passes=cfg["max_passes"], lod_voxel_size=cfg["lod"], deliver_to_host=deliver)
+        ids = [srv.add_client(w, h) for w, h in sizes]
+        return srv, ids
+
+    def closed_served(srv, ids, first, frames, cap_s):
+        """Every client keeps one frame outstanding; returns (frames, seconds)."""
+        count = [0] * nclients
+        t_end = time.perf_counter() + cap_s
+
+        def run(c):
+            for f in range(first, first + frames):
+                if time.perf_counter() > t_end:
+                    break
+                srv.wait(srv.submit(ids[c], cams[c][f]), timeout=cap_s + 60)
+                count[c] += 1
+        ts = [threading.Thread(target=run, args=(c,)) for c in range(nclients)]
+        srv.start()
+        t = time.perf_counter()
+        for th in ts:
+            th.start()
+        for th in ts:
+            th.join()
+        el = time.perf_counter() - t
+        srv.stop()
+        return sum(count), el
+
+    srv, ids = make_server(False)
+    closed_served(srv, ids, 0, args.warmup, 60)
+    log("served warm-up done")
+    barrier(world)
+    clocks = ClockSampler(local)
+    clocks.start()
+    n_served, el_served = closed_served(srv, ids, args.warmup, closed_frames, 60)
+    st = srv.stats()
+    srv.close()
+    log("served closed loop: %d frames in %.3fs" % (n_served, el_served))
+    srv, ids = make_server(True)
+    n_served_e2e, el_served_e2e = closed_served(srv, ids, args.warmup, closed_frames, 60)
+    log("served closed loop, delivered to host: %d frames in %.3fs" % (n_served_e2e, el_served_e2e))
+    # open loop: the Poisson schedule
+    reqs = []
+    srv.start()
+    t_start = time.perf_counter()
+    for (t, c, f) in sched:
+        dt = t_start + t - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        reqs.append(srv.submit(ids[c], cams[c][f]))
+    infos = [srv.wait(r, timeout=120) for r in reqs]
+    srv.stop()
+    sst = srv.stats()
+    srv.close()
+    lat_served = [(i["done_s"] - i["submit_s"]) * 1e3 for i in infos]
+    span_served = max(i["done_s"] for i in infos) - min(i["submit_s"] for i in infos)
+    log("served open loop: %d requests over %.3fs" % (len(infos), span_served))
+
+    # plain per-frame path: one renderer per client on the same cache
+    rts = []
+    for (w, h) in sizes:
+        rt = R.GPURayTracer(cm, w, h)
+        rt.set_lod_voxel_size(cfg["lod"])
+        rt.set_frame_time_limit(1e30)
+        rt.set_max_passes(cfg["max_passes"])
+        rts.append(rt)
+    pinned = [torch.empty((h, w, 4), dtype=torch.uint8).pin_memory() for w, h in sizes]
+
+    def plain_frame(c, f, deliver=True):
+        rts[c].RenderFrame(cams[c][f])
+        if deliver:
+            R._check(R.lib().rayt_renderer_read_image(rts[c]._h, pinned[c].data_ptr(), pinned[c].numel()))
+
+    def closed_plain(deliver, cap_s):
+        n, t_end = 0, time.perf_counter() + cap_s
+        t = time.perf_counter()
+        for f in range(args.warmup, args.warmup + closed_frames):
+            if time.perf_counter() > t_end:
+                break
+            for c in range(nclients):
+                plain_frame(c, f, deliver)
+                n += 1
+        torch.cuda.synchronize()
+        return n, time.perf_counter() - t
+
+    for c in range(nclients):
+        for f in range(args.warmup):
+            plain_frame(c, f)
+    n_plain, el_plain = closed_plain(False, 60)
+    n_plain_e2e, el_plain_e2e = closed_plain(True, 60)
+    log("plain closed loop: %d frames in %.3fs (%d in %.3fs delivered)" % (n_plain, el_plain, n_plain_e2e,
+                                                                           el_plain_e2e))
+    lat_plain = []
+    t_start = time.perf_counter()
+    for (t, c, f) in sched:
+        dt = t_start + t - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        plain_frame(c, f)
+        lat_plain.append((time.perf_counter() - (t_start + t)) * 1e3)
+        if time.perf_counter() - t_start > 60:
+            break
+    span_plain = time.perf_counter() - t_start
+    clk = clocks.stop()
+    log("plain open loop: %d of %d requests in %.3fs" % (len(lat_plain), len(sched), span_plain))
+
+    # roofline of the first pass on the largest client view
+    big = max(range(nclients), key=lambda c: pixels[c])
+    fetch = rts[big].count_fetches(cams[big][0])
+    pass_ms = rts[big].time_pass(cams[big][0], 3)
+    alg_bytes = 4 * fetch["link_fetches"] + 4 * fetch["far_fetches"] + 16 * fetch["rays"]
+    achieved = alg_bytes / (pass_ms / 1e3) / 1e9
+    peak, peak_kind = hbm_peak()
+    cpu = None
+    if rank == 0:
+        k, el = cpu_sample(args.cpu_seconds)
+        cpu = {"value": round(k / el, 3), "unit": "frames/s", "cores": threads, "kind": "port",
+               "sample": "%d %dx%d requests of the schedule (oracle, OpenMP)" % ((k,) + sizes[0])}
+        log("cpu sample done")
+    if rank != 0:
+        return None
+    sp50, sp99 = _pcts(lat_served)
+    pp50, pp99 = _pcts(lat_plain)
+    value = n_served / el_served
+    mean_px = sum(pixels) / nclients
+    return {
+        "metric": metric, "value": round(value, 2), "unit": "frames/s", "n_gpus": world,
+        "steps": n_served, "warmup": args.warmup, "ms_per_step": round(el_served / n_served * 1e3, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": wl, "clients": nclients, "depth": cfg["depth"], "spheres": cfg["spheres"],
+                   "nodes_in_block": cfg["nib"],
+                   "sizes": {"%dx%d" % k: sizes.count(k) for k in sorted(set(sizes))},
+                   "rate_hz_per_client": cfg["rate_hz"], "schedule_s": cfg["seconds"], "requests": len(sched),
+                   "cache_blocks": cap_blocks, "tree_blocks": ld.info.blocks_count, "blocks_loaded": loaded,
+                   "max_passes": cfg["max_passes"], "initial_fill_s": round(fill_s, 2),
+                   "l2": "inputs (the cache, GBs) larger than L2", "parallelism": "single GPU"},
+        "e2e": {"value": round(n_served_e2e / el_served_e2e, 2), "unit": "frames/s", "h2d_bytes_per_step": 64,
+                "d2h_bytes_per_step": int(mean_px * 4)},
+        "served": {"closed_loop_frames_s": round(value, 2),
+                   "closed_loop_mrays_s": round(n_served * mean_px / el_served / 1e6, 1),
+                   "open_loop": {"offered_frames_s": round(len(sched) / cfg["seconds"], 1),
+                                 "frames_s": round(len(infos) / span_served, 1), "p50_ms": sp50, "p99_ms": sp99,
+                                 "passes_mean": round(float(np.mean([i["passes"] for i in infos])), 3),
+                                 "truncated": int(sum(i["truncated"] for i in infos)),
+                                 "ticks": int(sst["ticks"])}},
+        "plain": {"closed_loop_frames_s": round(n_plain / el_plain, 2),
+                  "closed_loop_e2e_frames_s": round(n_plain_e2e / el_plain_e2e, 2),
+                  "closed_loop_mrays_s": round(n_plain * mean_px / el_plain / 1e6, 1),
+                  "open_loop": {"frames_s": round(len(lat_plain) / span_plain, 1), "p50_ms": pp50, "p99_ms": pp99,
+                                "served_requests": len(lat_plain)}},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+                     "kernel": "trace_kernel<first pass>, %dx%d client view" % sizes[big],
+                     "launch_ms": round(pass_ms, 4), "bytes_per_ray": round(alg_bytes / fetch["rays"], 2)},
+        "cpu_baseline": cpu, "gpu_launches": int(st["kernel_launches"]), "clocks": clk}
+
+
 # ---------------------------------------------------------------------------
 def zipf_words(n, seed=5, blocks=1 << 24, s=1.1):
     """C2 input: 90% NO_HIT, the rest block IDs ~ Zipf(s) over [0, blocks)
@@ -651,6 +926,8 @@ def main():
         out = bench_c2(args, rank, world, local)
     elif args.workload == "c4":
         out = bench_batched(args, rank, world, local)
+    elif args.workload == "c5":
+        out = bench_served(args, rank, world, local)
     else:
         out = bench_frames(args, rank, world, local)
     if rank == 0 and out is not None:

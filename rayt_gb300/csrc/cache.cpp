@@ -142,9 +142,10 @@ int Cache::Init(Tree* tree, int max_blocks) {
   nib_ = (int)tree->info.nodes_in_block;
   max_blocks_ = max_blocks > 0 ? max_blocks : (int)tree->info.blocks_count;
   const uint64_t nodes = (uint64_t)max_blocks_ * (uint64_t)nib_;
-  // cache-format limits: node indices are int in the feedback words, far
-  // pointer slots (index*8+i) must fit in 21 bits
-  if (nodes >= (1ull << 30)) return fail(RAYT_E_LIMIT, "cache holds >= 2^30 nodes (feedback words overflow)");
+  // cache-format limits: far pointer slots (index*8+i) must fit in 21 bits;
+  // node indices are int (the reference's per-pixel feedback word
+  // ((node+1)<<1)|dup needs node < 2^30, which only recorded passes build)
+  if (nodes >= (1ull << 31)) return fail(RAYT_E_LIMIT, "cache holds >= 2^31 nodes");
   if ((uint64_t)max_blocks_ * 8 >= (1ull << 21)) return fail(RAYT_E_LIMIT, "cache has >= 2^18 blocks (far pointer index overflows)");
   if (tree->chan_names.size() > (size_t)kMaxChannels) return fail(RAYT_E_LIMIT, "too many channels");
   RAYT_CUDA_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));

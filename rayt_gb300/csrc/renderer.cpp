@@ -409,6 +409,8 @@ int Renderer::Frame(const float* m) {
   const int64_t h2d0 = cache_->stats().bytes_h2d;
   int launches = 0;
   int64_t d2h = 0;
+  if (record && (uint64_t)cache_->max_blocks() * cache_->nodes_in_block() >= (1ull << 30))
+    return fail(RAYT_E_LIMIT, "recorded feedback words need a cache of fewer than 2^30 nodes");
   int rc = SetViews(m);
   if (rc != RAYT_OK) return rc;
   rc = cache_->StartSession();
