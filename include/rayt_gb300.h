@@ -336,7 +336,7 @@ int rayt_feedback_unique(const int32_t* device_words, int n, int nodes_in_block,
  * that owns all of HBM through its own allocator or reservation, or a frame
  * loop that cannot absorb the device-wide wait of cudaFree).  It calls no
  * cudaMalloc/cudaFree: its scratch is a fixed __device__ array of about
- * 16.5 MiB that each GPU loading the library keeps until exit, sized for n up
+ * 17 MiB that each GPU loading the library keeps until exit, sized for n up
  * to RAYT_FEEDBACK_UNIQUE_NOALLOC_MAX_WORDS (larger n returns RAYT_E_LIMIT).
  * All calls on a device share that array: calls whose GPU work overlaps race,
  * so order them on one stream or synchronise in between.  The first call on a

@@ -28,6 +28,8 @@ int get_scratch(size_t bytes, void** out) {
     }
     if (cudaMalloc(&s.ptr, bytes) != cudaSuccess) return fail(RAYT_E_OOM, "scratch allocation failed");
     s.bytes = bytes;
+    // the sort's look-back words are epoch-tagged, never cleared: start from zeros
+    RAYT_CUDA_TRY(cudaMemset(s.ptr, 0, bytes));
   }
   *out = s.ptr;
   return RAYT_OK;

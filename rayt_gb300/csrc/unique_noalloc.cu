@@ -13,7 +13,7 @@
 // Limits and sharing:
 //  * n is at most RAYT_FEEDBACK_UNIQUE_NOALLOC_MAX_WORDS (2^21 words, enough
 //    for the feedback of one 1920x1080 frame); larger n is rejected with
-//    RAYT_E_LIMIT before any GPU work.  The array is about 16.5 MiB and every
+//    RAYT_E_LIMIT before any GPU work.  The array is about 17 MiB and every
 //    GPU that loads the library holds it until the process exits.
 //  * Every call on a device uses the same array, so two calls whose GPU work
 //    overlaps (different streams, or different host threads without ordering)
@@ -21,8 +21,8 @@
 //    synchronise between them.  The array keeps the previous call's contents;
 //    every part the kernels expect to start at zero is cleared by each call.
 //  * The first call on each device looks up the array's device address with
-//    cudaGetSymbolAddress (with that device current); make that first call
-//    before any stream capture.
+//    cudaGetSymbolAddress and zeroes it once (with that device current); make
+//    that first call before any stream capture.
 // No cudaMalloc, cudaFree or allocating library routine is called here.
 #include <mutex>
 
@@ -37,12 +37,13 @@ constexpr size_t kCountsBytes = 256;
 // Sort/unique scratch for kMaxWords words plus 256 bytes for the result count.
 // feedback_scratch_bytes() is a host function, so the size is computed from the
 // same layout rules here: two key arrays of (n + 4) words rounded to 256 bytes,
-// 4 x 256 histogram words, one look-back word per 256 buckets per 4096-key
-// tile (+1 tile), 16 tile counters and 4 counts, each rounded to 256 bytes.
+// 4 x 256 histogram words, one 8-byte look-back word per 256 buckets per
+// 4096-key tile (+1 tile), 16 tile counters and 4 counts, each rounded to 256
+// bytes.
 constexpr size_t Up256(size_t v) { return (v + 255) & ~(size_t)255; }
 constexpr size_t kTiles = ((size_t)kMaxWords + 4095) / 4096 + 1;
 constexpr size_t kScratchBytes = 2 * Up256((size_t)kMaxWords * 4 + 16) + Up256(4 * 256 * 4) +
-                                 Up256(kTiles * 256 * 4) + Up256(16 * 4) + Up256(4 * 4);
+                                 Up256(kTiles * 256 * 8) + Up256(16 * 4) + Up256(4 * 4);
 
 static __device__ __align__(256) uint8_t g_noalloc_scratch[kScratchBytes + kCountsBytes];
 
@@ -58,6 +59,8 @@ int scratch_address(void** out) {
   if (!g_scratch_ptr[dev]) {
     void* p = nullptr;
     RAYT_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    // the sort's look-back words are epoch-tagged, never cleared: start from zeros
+    RAYT_CUDA_TRY(cudaMemset(p, 0, sizeof(g_noalloc_scratch)));
     g_scratch_ptr[dev] = p;
   }
   *out = g_scratch_ptr[dev];
