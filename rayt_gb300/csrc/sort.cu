@@ -102,13 +102,31 @@ SortScratchLayout layout(void* base, int n) {
 }
 
 // ---- compaction + histograms -------------------------------------------------
+// NodeToBlock's division of a node index (0 <= x < 2^31) by nodes_in_block d
+// without a hardware divide: q = floor(x * M / 2^64) with M = ceil(2^64 / d).
+// For x < 2^31 and d < 2^32 the product's excess x * (M - 2^64/d) / 2^64 is
+// below 1/d, so the floor equals floor(x / d) exactly (Granlund & Montgomery,
+// "Division by invariant integers using multiplication", 1994).  d = 1 passes
+// x through.
+struct Divider {
+  unsigned long long m;  // 0: d == 1
+};
+inline Divider make_divider(uint32_t d) {
+  Divider v;
+  v.m = d <= 1 ? 0ull : ~0ull / d + 1ull;
+  return v;
+}
+__device__ __forceinline__ uint32_t divide(uint32_t x, Divider v) {
+  return v.m ? (uint32_t)__umul64hi((unsigned long long)x, v.m) : x;
+}
+
 // Tiles of 4096 words, grid-strided.  A tile's kept keys go to one contiguous
 // range claimed with a single atomicAdd (order inside the tile by warp, then
 // round); the four 8-bit digit histograms of the kept keys build up in shared
 // memory on the way.
 template <bool kCompact>
-__global__ void __launch_bounds__(kThreads) compact_kernel(const int32_t* words, int n, int nib, uint32_t* keys,
-                                                           int* count, uint32_t* hist) {
+__global__ void __launch_bounds__(kThreads) compact_kernel(const int32_t* words, int n, int nib, Divider div,
+                                                           uint32_t* keys, int* count, uint32_t* hist) {
   __shared__ uint32_t sh[kPasses][kBuckets];
   __shared__ uint32_t s_warp[kWarps];
   __shared__ uint32_t s_base;
@@ -127,7 +145,7 @@ __global__ void __launch_bounds__(kThreads) compact_kernel(const int32_t* words,
       bool keep = i < n;
       if (kCompact) {
         keep = keep && w != kNoHit;
-        if (keep && w > 0 && nib > 0) w = ((((w >> 1) - 1) / nib + 1) << 1) | (w & 1);
+        if (keep && w > 0 && nib > 0) w = (int32_t)(((divide((uint32_t)((w >> 1) - 1), div) + 1) << 1) | (w & 1));
       }
       key[r] = (uint32_t)w ^ 0x80000000u;
       mask[r] = __ballot_sync(0xffffffffu, keep);
@@ -188,7 +206,7 @@ __global__ void hist_offsets_kernel(uint32_t* hist) {
 // ---- one stable counting pass over 8 bits ------------------------------------
 // Persistent: each CTA claims tiles in order from tile_counter until the
 // compacted keys run out, so the grid is the resident CTAs, not the input size.
-__global__ void __launch_bounds__(kThreads) digit_kernel(const uint32_t* in, uint32_t* out, const int* count,
+__global__ void __launch_bounds__(kThreads, 4) digit_kernel(const uint32_t* in, uint32_t* out, const int* count,
                                                          int shift, const uint32_t* digit_base,
                                                          unsigned long long* status, int* tile_counter, int pass,
                                                          bool last, int32_t* final_out) {
@@ -478,7 +496,8 @@ cudaError_t feedback_unique_device(const int32_t* words, int n, int nib, int32_t
   if ((e = cudaMemsetAsync(l.tile_counter, 0, 16 * 4, s)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(l.count, 0, 4 * 4, s)) != cudaSuccess) return e;
   const int grid = compact_grid(n);
-  compact_kernel<true><<<grid, kThreads, 0, s>>>(words, n, nib, l.keys_a, l.count, l.hist);
+  compact_kernel<true><<<grid, kThreads, 0, s>>>(words, n, nib, make_divider((uint32_t)nib), l.keys_a, l.count,
+                                                l.hist);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   uint32_t* cur = l.keys_a;
   uint32_t* other = l.keys_b;
@@ -497,7 +516,7 @@ cudaError_t sort_i32_device(int32_t* data, int n, void* scratch, size_t scratch_
   if ((e = cudaMemsetAsync(l.tile_counter, 0, 16 * 4, s)) != cudaSuccess) return e;
   if ((e = launch_fill_i32(l.count, n, 1, s)) != cudaSuccess) return e;
   const int grid = compact_grid(n);
-  compact_kernel<false><<<grid, kThreads, 0, s>>>(data, n, 0, l.keys_a, nullptr, l.hist);
+  compact_kernel<false><<<grid, kThreads, 0, s>>>(data, n, 0, make_divider(1), l.keys_a, nullptr, l.hist);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   uint32_t* cur = l.keys_a;
   uint32_t* other = l.keys_b;

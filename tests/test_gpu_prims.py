@@ -97,3 +97,19 @@ def test_feedback_unique_large_properties(built, n):
     conv[hit] = ((((conv[hit] >> 1) - 1) // 4096 + 1) << 1) | (conv[hit] & 1)
     np.testing.assert_array_equal(u, np.unique(conv).astype(np.int32))
     assert np.all(np.diff(u.astype(np.int64)) > 0) and u[-1] == NO_HIT
+
+
+@pytest.mark.parametrize("nib", [1, 2, 3, 7, 1000, 1024, 4096, 8192, 10000, 65535, 65536])
+def test_node_to_block_division_edges(built, nib):
+    """NodeToBlock divides node indices by nodes_in_block with a multiply-high;
+    node indices at block edges and up to 2^30 - 2 give the exact quotient."""
+    nodes = [0, 1, nib - 1, nib, nib + 1, 2 * nib - 1, (1 << 30) - 2, (1 << 30) - 3, 123456789, (1 << 29) + 7]
+    nodes += list(np.random.default_rng(nib).integers(0, (1 << 30) - 1, size=5000))
+    nodes = np.array([x for x in nodes if 0 <= x <= (1 << 30) - 2], np.int64)
+    dup = np.arange(nodes.size) & 1
+    words = (((nodes + 1) << 1) | dup).astype(np.int32)
+    words = np.concatenate([words, np.array([NO_HIT, -5, -1], np.int32)])
+    conv = words.astype(np.int64)
+    hit = (conv > 0) & (conv != NO_HIT)
+    conv[hit] = ((((conv[hit] >> 1) - 1) // nib + 1) << 1) | (conv[hit] & 1)
+    np.testing.assert_array_equal(_unique(words, nib), np.unique(conv).astype(np.int32))
