@@ -88,15 +88,19 @@ def parse():
 
 
 # ---------------------------------------------------------------------------
-def dist_setup(n):
+def dist_setup(n, backend="nccl"):
+    """Rank, world size and local rank from the torchrun environment; one
+    process group for the barrier and the timing reductions (NCCL on the GPU
+    box, gloo in the CPU tests)."""
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
     return rank, world, local
 
 
@@ -106,24 +110,25 @@ def barrier(world):
         dist.barrier()
 
 
-def max_over_ranks(x, world):
+def _reduce(x, world, op):
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=op)
     return float(t.item())
+
+
+def max_over_ranks(x, world):
+    import torch.distributed as dist
+    return _reduce(x, world, dist.ReduceOp.MAX) if world > 1 else x
 
 
 def sum_over_ranks(x, world):
-    if world == 1:
-        return x
-    import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    return _reduce(x, world, dist.ReduceOp.SUM) if world > 1 else x
 
 
 class ClockSampler:
