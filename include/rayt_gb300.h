@@ -244,6 +244,9 @@ typedef struct {
   int kernel_launches;       /* library kernels launched for the frame */
   int64_t bytes_h2d;         /* host->device bytes of the frame (block uploads) */
   int64_t bytes_d2h;         /* device->host bytes of the frame (feedback read-back) */
+  double host_ms_wait;       /* host time blocked on the GPU (pass synchronisations) */
+  double host_ms_decode;     /* host time in feedback decode, LRU marks and requests */
+  double host_ms_load;       /* host time in EndTransaction: block reads, linking, upload issue */
 } rayt_frame_stats;
 int rayt_renderer_stats(const rayt_renderer* r, rayt_frame_stats* out);
 

@@ -64,7 +64,8 @@ class FrameStats(C.Structure):
     _fields_ = [("passes", C.c_int), ("faults", C.c_int), ("uploaded_blocks", C.c_int), ("session_filled", C.c_int),
                 ("rays_traced", C.c_int64), ("gpu_ms_trace", C.c_float), ("gpu_ms_feedback", C.c_float),
                 ("gpu_ms_upload", C.c_float), ("frame_ms", C.c_double), ("kernel_launches", C.c_int),
-                ("bytes_h2d", C.c_int64), ("bytes_d2h", C.c_int64)]
+                ("bytes_h2d", C.c_int64), ("bytes_d2h", C.c_int64), ("host_ms_wait", C.c_double),
+                ("host_ms_decode", C.c_double), ("host_ms_load", C.c_double)]
 
 
 class ServerConfig(C.Structure):

@@ -32,7 +32,9 @@ namespace rayt {
 
 // Threads that read staged blocks from the file in parallel.  Run() returns
 // only after every item is done and every worker has left the job, so the
-// next Run() can reset the shared counters.
+// next Run() can reset the shared counters.  Wake() warns the pool that a job
+// is coming: sleeping workers get up and spin (bounded) until it arrives, so
+// the job does not pay for waking threads.
 class Cache::ReadPool {
  public:
   explicit ReadPool(int threads) {
@@ -46,6 +48,14 @@ class Cache::ReadPool {
     cv_.notify_all();
     for (auto& w : workers_) w.join();
   }
+  // Workers spin for up to `us` microseconds waiting for the next Run().
+  void Wake(int us) {
+    {
+      std::lock_guard<std::mutex> lock(mu_);
+      spin_until_ = Clock::now() + std::chrono::microseconds(us);
+    }
+    cv_.notify_all();
+  }
   // Runs fn(0..n-1) on the pool and the calling thread.
   void Run(int n, const std::function<void(int)>& fn) {
     if (n <= 0) return;
@@ -56,6 +66,7 @@ class Cache::ReadPool {
       next_.store(0);
       done_ = 0;
       ++gen_;
+      gen_seen_.store(gen_, std::memory_order_release);
     }
     cv_.notify_all();
     const int mine = Work(fn, n);
@@ -66,12 +77,15 @@ class Cache::ReadPool {
   }
 
  private:
+  using Clock = std::chrono::steady_clock;
   std::vector<std::thread> workers_;
   std::mutex mu_;
   std::condition_variable cv_, done_cv_;
   const std::function<void(int)>* fn_ = nullptr;
   int n_ = 0, done_ = 0, active_ = 0;
   uint64_t gen_ = 0;
+  std::atomic<uint64_t> gen_seen_{0};  // gen_, readable without the lock
+  Clock::time_point spin_until_{};
   std::atomic<int> next_{0};
   bool quit_ = false;
 
@@ -88,16 +102,25 @@ class Cache::ReadPool {
   void Loop() {
     uint64_t seen = 0;
     for (;;) {
-      const std::function<void(int)>* fn;
-      int n;
+      const std::function<void(int)>* fn = nullptr;
+      int n = 0;
+      Clock::time_point spin{};
       {
         std::unique_lock<std::mutex> lock(mu_);
-        cv_.wait(lock, [&] { return quit_ || (gen_ != seen && fn_); });
+        cv_.wait(lock, [&] { return quit_ || (gen_ != seen && fn_) || spin_until_ > Clock::now(); });
         if (quit_) return;
-        seen = gen_;
-        fn = fn_;
-        n = n_;
-        ++active_;
+        if (gen_ != seen && fn_) {
+          seen = gen_;
+          fn = fn_;
+          n = n_;
+          ++active_;
+        } else {
+          spin = spin_until_;
+        }
+      }
+      if (!fn) {  // woken ahead of a job: wait for it without sleeping
+        while (gen_seen_.load(std::memory_order_acquire) == seen && Clock::now() < spin) std::this_thread::yield();
+        continue;
       }
       const int finished = Work(*fn, n);
       {
@@ -549,6 +572,7 @@ int Cache::StartTransaction() {
   if (in_transaction_ || !in_session_) return fail(RAYT_E_STATE, "transaction needs an open session");
   in_transaction_ = true;
   InsertMarker(kTransaction);
+  pool_->Wake(500);  // the reads of EndTransaction follow the requests shortly
   return RAYT_OK;
 }
 int Cache::MarkBlockUsed(int slot) {

@@ -418,6 +418,8 @@ int Renderer::Frame(const float* m) {
   const int total = total_pixels_;
   int active_prev = total;  // rays traced by the first pass
   float ms_trace = 0, ms_fb = 0, ms_up = 0;
+  using clock = std::chrono::steady_clock;
+  auto ms_since = [](clock::time_point a) { return std::chrono::duration<double, std::milli>(clock::now() - a).count(); };
   int it;
   for (it = 0;; ++it) {
     if ((rc = RunPass(it, active_prev, &launches)) != RAYT_OK) break;
@@ -425,7 +427,9 @@ int Renderer::Frame(const float* m) {
       if (!h_dense_) RAYT_CUDA_TRY(cudaHostAlloc(&h_dense_, (size_t)padded_pixels_ * 4, cudaHostAllocDefault));
       RAYT_CUDA_TRY(cudaMemcpyAsync(h_dense_, d_dense_, (size_t)padded_pixels_ * 4, cudaMemcpyDeviceToHost, s_));
     }
+    const auto tw = clock::now();
     RAYT_CUDA_TRY(cudaStreamSynchronize(s_));
+    stats.host_ms_wait += ms_since(tw);
     float a = 0, b = 0;
     cudaEventElapsedTime(&a, ev_[0], ev_[1]);
     cudaEventElapsedTime(&b, ev_[1], ev_[2]);
@@ -447,6 +451,7 @@ int Renderer::Frame(const float* m) {
     if (it > 0 && el > time_limit) { active_prev = active_now; break; }
     if (max_passes > 0 && it > 0 && it + 1 >= max_passes) { active_prev = active_now; break; }
 
+    const auto td = clock::now();
     fb_.Decode(h_unique_, h_counts_[0], rand);
     if ((rc = cache_->StartTransaction()) != RAYT_OK) break;
     for (int b2 : fb_.hits) cache_->MarkBlockUsed(b2);
@@ -456,8 +461,11 @@ int Renderer::Frame(const float* m) {
       if ((rc = cache_->RequestBlock(f)) != RAYT_OK) break;
     }
     stats.faults += (int)fb_.faults.size();
+    stats.host_ms_decode += ms_since(td);
     RAYT_CUDA_TRY(cudaEventRecord(ev_[3], s_));
+    const auto tl = clock::now();
     const int erc = cache_->EndTransaction();
+    stats.host_ms_load += ms_since(tl);
     RAYT_CUDA_TRY(cudaEventRecord(ev_[4], s_));
     if (rc == RAYT_OK) rc = erc;
     if (rc != RAYT_OK) break;
@@ -480,7 +488,9 @@ int Renderer::Frame(const float* m) {
   f.n_in = p.n_out;
   RAYT_CUDA_TRY(launch_finish(f, active_prev, s_));
   if (active_prev > 0) ++launches;
+  const auto tw = clock::now();
   RAYT_CUDA_TRY(cudaStreamSynchronize(s_));
+  stats.host_ms_wait += ms_since(tw);
   if (stats.passes > 1 || stats.faults) {
     float up = 0;
     if (cudaEventElapsedTime(&up, ev_[3], ev_[4]) == cudaSuccess) ms_up += up;
