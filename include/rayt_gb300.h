@@ -178,6 +178,13 @@ void rayt_renderer_destroy(rayt_renderer* r);
 /* set_frame_time_limit / set_lod_voxel_size (gpu-ray-tracer.h:17-23). */
 int rayt_renderer_set_frame_time_limit(rayt_renderer* r, double seconds);
 int rayt_renderer_set_lod_voxel_size(rayt_renderer* r, float size);
+/* No counterpart in the reference (its todo list, msvs/rayt/todo.txt:5:
+ * "Decrease LOD when cache is too small").  When on, a frame whose session
+ * filled the cache makes the next frame render with grow x the voxel size (at
+ * most max_lod_voxel_size); a frame that did not shrinks it by shrink, down to
+ * the size set with rayt_renderer_set_lod_voxel_size.  Off by default;
+ * rayt_frame_stats.lod_voxel_size reports the size each frame used. */
+int rayt_renderer_set_lod_pressure(rayt_renderer* r, int on, float max_lod_voxel_size, float grow, float shrink);
 /* Deterministic frame end: at most max_passes tracing passes (0 = no cap).  The
  * cap is applied where the reference applies its wall-clock limit. */
 int rayt_renderer_set_max_passes(rayt_renderer* r, int max_passes);
@@ -247,9 +254,18 @@ typedef struct {
   double host_ms_wait;       /* host time blocked on the GPU (pass synchronisations) */
   double host_ms_decode;     /* host time in feedback decode, LRU marks and requests */
   double host_ms_load;       /* host time in EndTransaction: block reads, linking, upload issue */
+  float lod_voxel_size;      /* the LOD voxel size the frame rendered with */
 } rayt_frame_stats;
 int rayt_renderer_stats(const rayt_renderer* r, rayt_frame_stats* out);
 
+/* The reference's debug depth view (RaytraceKernel, rayt/GPU_renderer/kernels/
+ * raytracer.cl:18-71, not wired into its application): rays from the near
+ * plane, one pass over the cache as it is, no feedback or loads.  RGBA8 into
+ * device_rgba (width x height, row 0 at the bottom): red where a ray faults or
+ * errs, black where it misses, else grey = 255 * (1 - log-depth in [0.01, 5]).
+ * Runs on `stream` (null: the cache's stream) and returns when done. */
+int rayt_cache_depth_view(rayt_cache* cache, const float view_proj_inv[16], float lod_voxel_size, int width,
+                          int height, void* device_rgba, void* stream);
 /* Traces one pass from view_proj_inv (one matrix per view) against the cache
  * as it is (no feedback, no uploads) and counts node-link and far-pointer
  * fetches: the algorithmic byte count of the traversal roofline.  counts =

@@ -38,7 +38,7 @@ SRC=(
   "$REF/scene/camera.cpp" "$REF/scene sources/stored-octree-test.cpp"
   "$HERE/ref_harness/fake_cl.cpp" "$HERE/ref_harness/stopwatch_linux.cpp"
   "$HERE/ref_harness/cl_init.cpp" "$HERE/ref_harness/cl_pass.cpp" "$HERE/ref_harness/cl_finish.cpp"
-  "$HERE/ref_harness/cl_feedback.cpp" "$HERE/ref_harness/cl_sort_scan.cpp"
+  "$HERE/ref_harness/cl_feedback.cpp" "$HERE/ref_harness/cl_sort_scan.cpp" "$HERE/ref_harness/cl_depth.cpp"
   "$HERE/ref_harness/ref_api.cpp"
 )
 

@@ -43,6 +43,7 @@ def lib():
             "oracle_frame_pass_words": (i32, [vp, i32, vp]),
             "oracle_renderer_counters": (None, [vp, C.POINTER(C.c_longlong)]),
             "oracle_trace_once": (i32, [vp, C.POINTER(C.c_float), vp, vp]),
+            "oracle_depth_view": (i32, [vp, C.POINTER(C.c_float), C.c_float, i32, i32, vp]),
             "oracle_sort": (None, [vp, i32]),
             "oracle_scan": (None, [vp, i32]),
             "oracle_feedback_unique": (i32, [vp, i32, i32, vp]),
@@ -126,6 +127,13 @@ class OracleScene:
         rgba = np.zeros((self.h, self.w, 4), np.uint8)
         lib().oracle_trace_once(self.r, p, words.ctypes.data, rgba.ctypes.data)
         return words, rgba
+
+    def depth_view(self, mat, lod, w, h):
+        """raytracer.cl's debug depth view over the cache as it is."""
+        m, p = _m(mat)
+        out = np.zeros((h, w, 4), np.uint8)
+        lib().oracle_depth_view(self.cache, p, lod, w, h, out.ctypes.data)
+        return out
 
     def counters(self):
         out = (C.c_longlong * 6)()

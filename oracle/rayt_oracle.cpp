@@ -483,6 +483,49 @@ void Cast(const uint32_t* links, const uint32_t* far, int root, V4 p, V4 d, floa
   r->t = 1e30f; r->node = -1; r->iterations = iter;
 }
 
+// raytracer.cl:18-71 (RaytraceKernel, the reference's debug depth view): one
+// pass from the near plane over the cache as it is, no feedback; red for a
+// fault or error, black for a miss, else grey = 255 * (1 - log-depth in
+// [0.01, 5]).  The grey conversion clamps to [0, 255] (the reference's
+// conversion is undefined outside that range).
+void DepthView(const uint32_t* links, const uint32_t* far, int root, uint32_t node_limit, uint32_t far_limit,
+               const float* m, float lod, int W, int H, uint8_t* out) {
+#pragma omp parallel for schedule(dynamic, 256)
+  for (long long i = 0; i < (long long)W * H; ++i) {
+    const int x = (int)(i % W), y = (int)(i / W);
+    V4 tmp = v4((x + 0.5f) / W * 2 - 1, (y + 0.5f) / H * 2 - 1, -1, 0);
+    const V4 origin = MulPoint(m, tmp);
+    tmp.z = 0;
+    V4 dir = Sub(MulPoint(m, tmp), origin);
+    dir = Div(dir, Len(dir));
+    tmp = v4((float)x / W * 2 - 1, (float)y / H * 2 - 1, -1, 0);
+    const V4 p1n = MulPoint(m, tmp);
+    tmp.z = 0;
+    const V4 p1f = MulPoint(m, tmp);
+    tmp = v4((float)(x + 1) / W * 2 - 1, (float)(y + 1) / H * 2 - 1, -1, 0);
+    const V4 p2n = MulPoint(m, tmp);
+    tmp.z = 0;
+    const V4 p2f = MulPoint(m, tmp);
+    const float bias = lod * Len(Sub(p1n, p2n));
+    const float coef = (bias < 1e-10f) ? 0 : (lod * (Len(Sub(p1f, p2f)) - Len(Sub(p1n, p2n))) / Len(Sub(p1n, p1f)));
+    CastResult r{};
+    Cast(links, far, root, origin, dir, coef, bias, &r, node_limit, far_limit);
+    uint8_t* o = out + i * 4;
+    if (r.error || r.fault_block != -1) {
+      o[0] = 255, o[1] = 0, o[2] = 0, o[3] = 255;
+    } else if (r.node == -1) {
+      o[0] = 0, o[1] = 0, o[2] = 0, o[3] = 255;
+    } else {
+      const float near_ = 0.01f, far_ = 5;
+      float d = (std::log(r.t) - std::log(near_)) / (std::log(far_) - std::log(near_));
+      d = (1 - d) * 255;
+      d = std::min(255.0f, std::max(0.0f, d));
+      const uint8_t g = (uint8_t)d;
+      o[0] = g, o[1] = g, o[2] = g, o[3] = 255;
+    }
+  }
+}
+
 // shading.cl:4-33
 void Shade(int node, RayState& s, const int8_t* normals, const uint8_t* colors) {
   static const V4 L1 = [] { V4 v = v4(2, -2, 3, 0); V4 n = Div(v, Len(v)); return v4(n.x * .6f, n.y * .6f, n.z * .6f, n.w * .6f); }();
@@ -900,6 +943,13 @@ int oracle_trace_once(void* rp, const float* m, int* words_out, unsigned char* r
       FinishPixel(s, nrm, col, rgba_out + (size_t)i * 4);
     }
   }
+  return 0;
+}
+
+int oracle_depth_view(void* cp, const float* m, float lod, int w, int h, unsigned char* out) {
+  Cache* c = static_cast<Cache*>(cp);
+  DepthView(c->links(), c->far.data(), c->root_node, (uint32_t)c->max_blocks * (uint32_t)c->nib,
+            (uint32_t)c->max_blocks * 8u, m, lod, w, h, out);
   return 0;
 }
 

@@ -11,6 +11,8 @@
 //   distance(a, b) = length(a - b)
 //   vector / scalar is a component-wise IEEE divide (not a reciprocal multiply)
 //   min/max(x, y)  = OpenCL definitions: y < x ? y : x and x < y ? y : x
+//   log(x)         = the C library's logf (OpenCL allows 3 ulp; only the debug
+//                    depth view uses it, and is compared within 1 LSB)
 // The kernels are built with -ffp-contract=off so no multiply-add is fused.
 #pragma once
 #include <cmath>
@@ -71,6 +73,7 @@ inline float copysign(float a, float b) { return std::copysign(a, b); }
 inline float fmin(float a, float b) { return std::fmin(a, b); }
 inline float fmax(float a, float b) { return std::fmax(a, b); }
 inline float sqrt(float v) { return std::sqrt(v); }
+inline float log(float v) { return std::log(v); }  // natural log in float (libm logf)
 inline float min(float a, float b) { return b < a ? b : a; }
 inline float max(float a, float b) { return a < b ? b : a; }
 inline int min(int a, int b) { return b < a ? b : a; }

@@ -17,6 +17,8 @@
 #include "../../rayt_gb300/csrc/scene_source.h"
 
 extern std::function<void(const std::string&, const clc::Args&)> g_fakecl_after_kernel;
+void refcl_depth_view(unsigned char* rgba, const unsigned* links, const unsigned* fars, int root,
+                      const float* view_proj_inv, float lod_voxel_size, int w, int h);
 
 using namespace rayt;
 
@@ -133,6 +135,20 @@ int ref_session_read(void* p, const char* name, void* out, long long bytes) {
     b = s->cache->data()->ChannelByName(name)->cl_buffer();
   if (!b || bytes > b->size()) return -1;
   b->Read(0, (int)bytes, out);
+  return 0;
+}
+
+// RaytraceKernel (raytracer.cl, the reference's debug depth view) over the
+// session's cache as it is: RGBA8, w x h.
+int ref_session_depth_view(void* p, const float* view_proj_inv, float lod_voxel_size, int w, int h,
+                           unsigned char* out) {
+  Session* s = static_cast<Session*>(p);
+  const CLBuffer* lb = s->cache->data()->ChannelByName("node links")->cl_buffer();
+  const CLBuffer* fb = s->cache->data()->far_pointers_buffer();
+  std::vector<unsigned> links(lb->size() / 4), fars(fb->size() / 4);
+  lb->Read(0, (int)lb->size(), links.data());
+  fb->Read(0, (int)fb->size(), fars.data());
+  refcl_depth_view(out, links.data(), fars.data(), s->cache->root_node_index(), view_proj_inv, lod_voxel_size, w, h);
   return 0;
 }
 

@@ -65,7 +65,7 @@ class FrameStats(C.Structure):
                 ("rays_traced", C.c_int64), ("gpu_ms_trace", C.c_float), ("gpu_ms_feedback", C.c_float),
                 ("gpu_ms_upload", C.c_float), ("frame_ms", C.c_double), ("kernel_launches", C.c_int),
                 ("bytes_h2d", C.c_int64), ("bytes_d2h", C.c_int64), ("host_ms_wait", C.c_double),
-                ("host_ms_decode", C.c_double), ("host_ms_load", C.c_double)]
+                ("host_ms_decode", C.c_double), ("host_ms_load", C.c_double), ("lod_voxel_size", C.c_float)]
 
 
 class ServerConfig(C.Structure):
@@ -136,6 +136,7 @@ def lib():
         "rayt_renderer_seed": (i32, [vp, u32]),
         "rayt_renderer_record_passes": (i32, [vp, i32]),
         "rayt_renderer_use_graphs": (i32, [vp, i32]),
+        "rayt_renderer_set_lod_pressure": (i32, [vp, i32, f32, f32, f32]),
         "rayt_render_frame": (i32, [vp, C.POINTER(f32)]),
         "rayt_renderer_image": (i32, [vp, C.POINTER(vp)]),
         "rayt_renderer_stream": (i32, [vp, C.POINTER(vp)]),
@@ -152,6 +153,7 @@ def lib():
         "rayt_renderer_set_launch_shape": (i32, [vp, i32, i32, i32, i32]),
         "rayt_renderer_get_launch_shape": (i32, [vp, C.POINTER(i32)]),
         "rayt_renderer_autotune": (i32, [vp, C.POINTER(f32), i32, C.POINTER(i32)]),
+        "rayt_cache_depth_view": (i32, [vp, C.POINTER(f32), f32, i32, i32, vp, vp]),
         "rayt_server_create": (i32, [vp, C.POINTER(ServerConfig), C.POINTER(vp)]),
         "rayt_server_destroy": (None, [vp]),
         "rayt_server_add_client": (i32, [vp, i32, i32, C.POINTER(i32)]),
@@ -296,6 +298,19 @@ class GPUOctreeCacheManager:
         _check(lib().rayt_cache_blocks(self._h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
+    def depth_view(self, view_proj_inv, lod_voxel_size, width, height, device_out=None):
+        """raytracer.cl's debug depth view over the cache as it is; returns an
+        (height, width, 4) uint8 array (or fills a device buffer with a
+        data_ptr() and returns it)."""
+        m, p = _mat(view_proj_inv)
+        if device_out is not None:
+            _check(lib().rayt_cache_depth_view(self._h, p, lod_voxel_size, width, height, _ptr(device_out), None))
+            return device_out
+        import torch
+        buf = torch.empty((height, width, 4), dtype=torch.uint8, device="cuda")
+        _check(lib().rayt_cache_depth_view(self._h, p, lod_voxel_size, width, height, buf.data_ptr(), None))
+        return buf.cpu().numpy()
+
     def read_buffer(self, name, dtype=np.uint8):
         size = C.c_size_t()
         ptr = C.c_void_p()
@@ -393,6 +408,11 @@ class GPURayTracer:
 
     def seed(self, seed):
         _check(lib().rayt_renderer_seed(self._h, seed))
+
+    def set_lod_pressure(self, on=True, max_lod_voxel_size=16.0, grow=1.5, shrink=1.25):
+        """Coarser LOD after frames whose session filled the cache (see
+        rayt_renderer_set_lod_pressure)."""
+        _check(lib().rayt_renderer_set_lod_pressure(self._h, 1 if on else 0, max_lod_voxel_size, grow, shrink))
 
     def use_graphs(self, on=True):
         _check(lib().rayt_renderer_use_graphs(self._h, 1 if on else 0))

@@ -111,6 +111,8 @@ cudaError_t trace_node_params(const TraceParams* p, bool first, bool count, int 
 int trace_persistent_grid(bool first, bool count);
 cudaError_t launch_finish(const TraceParams& p, int max_rays, cudaStream_t s);
 cudaError_t launch_fill_i32(int* p, int32_t v, size_t n, cudaStream_t s);
+// The reference's debug depth view (raytracer.cl) of views[0] into image.
+cudaError_t launch_depth_view(const TraceParams& p, cudaStream_t s);
 
 // Feedback bitmaps -> the reference's sorted unique array.
 struct UniqueFromBitsParams {

@@ -38,7 +38,14 @@ class Renderer {
   int PassWords(int pass, int32_t* host, size_t count) const;
 
   double time_limit = 1.0;  // the reference's default (gpu-ray-tracer.cpp:30-31)
-  float lod = 1.5f;
+  float lod = 1.5f;         // lod_voxel_size set by the caller
+  float lod_used = 1.5f;    // the one frames render with (differs under LOD pressure)
+  // LOD under cache pressure (the reference's todo "Decrease LOD when cache is
+  // too small", msvs/rayt/todo.txt:5): after a frame whose session filled the
+  // cache, the next frame's voxel size grows by `grow` (at most `max`); after a
+  // frame that did not, it shrinks back by `shrink` (at least `lod`).
+  bool lod_pressure = false;
+  float lod_max = 16.0f, lod_grow = 1.5f, lod_shrink = 1.25f;
   int max_passes = 0;
   bool record = false;
   LibcRand rand;
@@ -193,7 +200,7 @@ int Renderer::SetViews(const float* m) {
     for (int v = g * kViewsPerLaunch; v < end; ++v) {
       ViewDesc& d = views_[v];
       std::memcpy(d.m, m + 16 * v, sizeof(d.m));
-      d.lod = lod;
+      d.lod = lod_used;
       d.tiles_x = (d.width + tw - 1) / tw;
       d.tile_base = (int)std::min<int64_t>(tiles, INT32_MAX);
       tiles += (int64_t)d.tiles_x * ((d.height + th - 1) / th);
@@ -474,6 +481,11 @@ int Renderer::Frame(const float* m) {
   }
   stats.passes = it + 1;
   stats.session_filled = cache_->in_session() && cache_->SessionFilled() ? 1 : 0;
+  stats.lod_voxel_size = lod_used;
+  if (lod_pressure) {
+    if (stats.session_filled) lod_used = std::min(lod_max, lod_used * lod_grow);
+    else if (lod_used > lod) lod_used = std::max(lod, lod_used / lod_shrink);
+  }
   if (cache_->in_transaction()) cache_->EndTransaction();
   const int src = cache_->EndSession();
   if (rc != RAYT_OK) return rc;
@@ -636,6 +648,17 @@ int rayt_renderer_set_frame_time_limit(rayt_renderer* r, double s) {
 int rayt_renderer_set_lod_voxel_size(rayt_renderer* r, float v) {
   if (!r || !(v >= 0)) return fail(RAYT_E_ARG, "bad LOD voxel size");
   R(r)->lod = v;
+  R(r)->lod_used = v;
+  return RAYT_OK;
+}
+int rayt_renderer_set_lod_pressure(rayt_renderer* r, int on, float max_lod_voxel_size, float grow, float shrink) {
+  if (!r || !(grow >= 1) || !(shrink >= 1) || !(max_lod_voxel_size >= 0)) return fail(RAYT_E_ARG, "bad LOD pressure settings");
+  rayt::Renderer* q = R(r);
+  q->lod_pressure = on != 0;
+  q->lod_max = max_lod_voxel_size;
+  q->lod_grow = grow;
+  q->lod_shrink = shrink;
+  if (!q->lod_pressure) q->lod_used = q->lod;
   return RAYT_OK;
 }
 int rayt_renderer_set_max_passes(rayt_renderer* r, int n) {
@@ -726,6 +749,31 @@ int rayt_renderer_pass_words(rayt_renderer* r, int pass, int32_t* host, size_t c
 int rayt_renderer_stats(const rayt_renderer* r, rayt_frame_stats* out) {
   if (!r || !out) return fail(RAYT_E_ARG, "null argument");
   *out = reinterpret_cast<const rayt::Renderer*>(r)->stats;
+  return RAYT_OK;
+}
+int rayt_cache_depth_view(rayt_cache* cache, const float view_proj_inv[16], float lod_voxel_size, int width,
+                          int height, void* device_rgba, void* stream) {
+  if (!cache || !view_proj_inv || !device_rgba) return fail(RAYT_E_ARG, "rayt_cache_depth_view: null argument");
+  if (width <= 0 || height <= 0 || (int64_t)width * height >= (1ll << 31) || !(lod_voxel_size >= 0))
+    return fail(RAYT_E_ARG, "rayt_cache_depth_view: bad size or LOD");
+  rayt::Cache* c = reinterpret_cast<rayt::Cache*>(cache);
+  rayt::TraceParams p;
+  std::memset(&p, 0, sizeof(p));
+  p.links = c->links();
+  p.far_ptrs = c->far_ptrs();
+  p.root = c->root_node();
+  p.nodes_in_block = c->nodes_in_block();
+  p.node_limit = (uint32_t)c->max_blocks() * (uint32_t)c->nodes_in_block();
+  p.far_limit = (uint32_t)c->max_blocks() * 8u;
+  p.image = static_cast<uchar4*>(device_rgba);
+  p.n_views = 1;
+  std::memcpy(p.views[0].m, view_proj_inv, sizeof(p.views[0].m));
+  p.views[0].width = width;
+  p.views[0].height = height;
+  p.views[0].lod = lod_voxel_size;
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream();
+  RAYT_CUDA_TRY(rayt::launch_depth_view(p, s));
+  RAYT_CUDA_TRY(cudaStreamSynchronize(s));
   return RAYT_OK;
 }
 int rayt_renderer_count_fetches(rayt_renderer* r, const float* m, int64_t counts[6]) {

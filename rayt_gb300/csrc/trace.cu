@@ -714,6 +714,57 @@ __global__ void __launch_bounds__(kBlockThreads) finish_kernel(const __grid_cons
   p.image[p.in_ray[i]] = finish(p, col);
 }
 
+// raytracer.cl:18-71 (RaytraceKernel, the reference's debug depth view) for
+// view 0 of the parameters: rays from the near plane, one pass over the cache
+// as it is, no feedback.  Red for a fault or an error, black for a miss, else
+// grey = 255 * (1 - log-depth in [0.01, 5]) clamped to [0, 255] (the
+// reference's float-to-uchar conversion is undefined outside that range).
+__global__ void __launch_bounds__(kBlockThreads) depth_view_kernel(const __grid_constant__ TraceParams p) {
+  const ViewDesc& v = p.views[0];
+  const int W = v.width, H = v.height;
+  const int i = blockIdx.x * kBlockThreads + threadIdx.x;
+  if (i >= W * H) return;
+  const int x = i % W, y = i / W;
+  const float cx = __fdiv_rn(x + 0.5f, (float)W) * 2 - 1, cy = __fdiv_rn(y + 0.5f, (float)H) * 2 - 1;
+  float o[4], q[4], p1n[4], p1f[4], p2n[4], p2f[4];
+  mul_point(v.m, cx, cy, -1.0f, o);
+  mul_point(v.m, cx, cy, 0.0f, q);
+  float dx = q[0] - o[0], dy = q[1] - o[1], dz = q[2] - o[2], dw = q[3] - o[3];
+  const float len = __fsqrt_rn(dot4(dx, dy, dz, dw, dx, dy, dz, dw));
+  dx = __fdiv_rn(dx, len);
+  dy = __fdiv_rn(dy, len);
+  dz = __fdiv_rn(dz, len);
+  const float ax = __fdiv_rn((float)x, (float)W) * 2 - 1, ay = __fdiv_rn((float)y, (float)H) * 2 - 1;
+  const float bx = __fdiv_rn((float)(x + 1), (float)W) * 2 - 1, by = __fdiv_rn((float)(y + 1), (float)H) * 2 - 1;
+  mul_point(v.m, ax, ay, -1.0f, p1n);
+  mul_point(v.m, ax, ay, 0.0f, p1f);
+  mul_point(v.m, bx, by, -1.0f, p2n);
+  mul_point(v.m, bx, by, 0.0f, p2f);
+  auto dist = [](const float* a, const float* b) {
+    const float ex = a[0] - b[0], ey = a[1] - b[1], ez = a[2] - b[2], ew = a[3] - b[3];
+    return __fsqrt_rn(dot4(ex, ey, ez, ew, ex, ey, ez, ew));
+  };
+  const float bias = v.lod * dist(p1n, p2n);
+  const float coef = bias < 1e-10f ? 0.0f : __fdiv_rn(v.lod * (dist(p1f, p2f) - dist(p1n, p2n)), dist(p1n, p1f));
+  uint32_t fetches = 0, far_fetches = 0;
+  const RayEnd e = cast_ray<false>(p, make_float4(o[0], o[1], o[2], bias), make_float4(dx, dy, dz, coef), fetches,
+                                   far_fetches);
+  uchar4 c;
+  if (e.error || e.fault_block != -1) {
+    c = make_uchar4(255, 0, 0, 255);
+  } else if (e.node == -1) {
+    c = make_uchar4(0, 0, 0, 255);
+  } else {
+    const float near_ = 0.01f, far_ = 5.0f;
+    float d = __fdiv_rn(logf(e.t) - logf(near_), logf(far_) - logf(near_));
+    d = (1 - d) * 255;
+    d = fminf(255.0f, fmaxf(0.0f, d));
+    const unsigned char g = (unsigned char)d;
+    c = make_uchar4(g, g, g, 255);
+  }
+  p.image[i] = c;
+}
+
 __global__ void fill_kernel(int* p, int32_t v, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) p[i] = v;
 }
@@ -874,6 +925,13 @@ cudaError_t unique_node_params(const UniqueFromBitsParams* q, void** args, cudaK
 cudaError_t launch_finish(const TraceParams& p, int max_rays, cudaStream_t s) {
   if (max_rays <= 0) return cudaSuccess;
   finish_kernel<<<(max_rays + kBlockThreads - 1) / kBlockThreads, kBlockThreads, 0, s>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_depth_view(const TraceParams& p, cudaStream_t s) {
+  const long long n = (long long)p.views[0].width * p.views[0].height;
+  if (n <= 0) return cudaSuccess;
+  depth_view_kernel<<<(unsigned)((n + kBlockThreads - 1) / kBlockThreads), kBlockThreads, 0, s>>>(p);
   return cudaGetLastError();
 }
 

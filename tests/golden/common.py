@@ -75,6 +75,18 @@ FRAME_CASES = {
                               [200.0, -35.0, 0.0, 0.9, 0.7, -0.1, 60.0]]},
 }
 
+# raytracer.cl's debug depth view over the cache right after InitialFillCache
+# (resident trees, and a partial cache whose faults show red)
+DEPTH_CASES = {
+    "resident_c1": {"tree": "terrain10", "max_blocks": 0, "size": [160, 120], "lod": 1.0, "camera": C1_CAMERA},
+    "resident_lod0": {"tree": "terrain10", "max_blocks": 0, "size": [96, 80], "lod": 0.0,
+                      "camera": [30.0, -25.0, 0.0, 0.1, 0.6, 1.1, 60.0]},
+    "partial8s": {"tree": "terrain8s", "max_blocks": 60, "size": [128, 72], "lod": 1.0,
+                  "camera": [80.0, -40.0, 5.0, 0.0, 0.8, 0.7, 70.0]},
+    "sphere_lod4": {"tree": "sphere7", "max_blocks": 0, "size": [64, 64], "lod": 4.0,
+                    "camera": [200.0, -35.0, 0.0, 0.9, 0.7, -0.1, 60.0]},
+}
+
 
 def _splitmix(x):
     x = (x + np.uint64(0x9E3779B97F4A7C15)) & np.uint64(0xFFFFFFFFFFFFFFFF)

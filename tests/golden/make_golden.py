@@ -20,7 +20,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
-from tests.golden.common import (BUILDER_CASES, FRAME_CASES, SPHERE_CACHE_CASES, canonical_tree_bytes,  # noqa: E402
+from tests.golden.common import (BUILDER_CASES, DEPTH_CASES, FRAME_CASES, SPHERE_CACHE_CASES, canonical_tree_bytes,  # noqa: E402
                                  feedback_words, sha)
 
 REF = os.path.join(ROOT, "oracle", "_ref", "librayt_ref.so")
@@ -48,6 +48,7 @@ def load_ref():
     L.ref_sort.argtypes = [vp, C.c_int]
     L.ref_scan.argtypes = [vp, C.c_int]
     L.ref_feedback_unique.argtypes = [vp, C.c_int, C.c_int, vp]
+    L.ref_session_depth_view.argtypes = [vp, vp, C.c_float, C.c_int, C.c_int, vp]
     return L
 
 
@@ -131,6 +132,20 @@ def main():
             golden["frames"][name] = frames
             L.ref_renderer_destroy(r)
             L.ref_session_close(s)
+        # the debug depth view (raytracer.cl) over freshly filled caches
+        depth = {}
+        for name, case in DEPTH_CASES.items():
+            path = os.path.join(tmp, case["tree"] + ".tree")
+            s = L.ref_session_open(path.encode(), case["max_blocks"])
+            w, h = case["size"]
+            m = np.zeros(16, np.float32)
+            cam_arr = np.array(case["camera"] + [w / h], np.float32)
+            L.ref_camera_matrix(cam_arr.ctypes.data, m.ctypes.data)
+            img = np.zeros((h, w, 4), np.uint8)
+            L.ref_session_depth_view(s, m.ctypes.data, case["lod"], w, h, img.ctypes.data)
+            depth[name + "_matrix"] = m
+            depth[name + "_image"] = img
+            L.ref_session_close(s)
         # GPUSort / GPUScan known-answer runs (test-application.cpp:150-240):
         # n = 2013, values rand() % 201 - 100 after srand(seed), 10 trials
         L.ref_srand(12345)
@@ -163,6 +178,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "sort_scan.npz"), inputs=np.stack(sort_in), sorted=np.stack(sort_out),
                         scanned=np.stack(scan_out))
     np.savez_compressed(os.path.join(HERE, "feedback_unique.npz"), **fb)
+    np.savez_compressed(os.path.join(HERE, "depth_views.npz"), **depth)
     if images:
         np.savez_compressed(os.path.join(HERE, "frame_images.npz"), **images)
     print("wrote golden fixtures to", HERE)

@@ -144,3 +144,49 @@ def test_pass_cap_stops_frame(trees):
     rt.set_max_passes(2)
     rt.RenderFrame(m)
     assert rt.stats()["passes"] <= 2
+
+
+@pytest.mark.parametrize("name", sorted(__import__("tests.golden.common", fromlist=["DEPTH_CASES"]).DEPTH_CASES))
+def test_depth_view_matches_reference(trees, name):
+    """rayt_cache_depth_view against the reference's raytracer.cl run by the
+    harness: red (fault/error) and black (miss) exact, grey within 1 LSB
+    (CUDA's logf against the C library's)."""
+    from tests.golden.common import DEPTH_CASES
+    case = DEPTH_CASES[name]
+    d = np.load(os.path.join(GOLDEN, "depth_views.npz"))
+    w, h = case["size"]
+    ld = R.StoredOctreeLoader(trees[case["tree"]])
+    cm = R.GPUOctreeCacheManager(case["max_blocks"], ld)
+    cm.InitialFillCache()
+    img = cm.depth_view(d[name + "_matrix"], case["lod"], w, h)
+    ref = d[name + "_image"]
+    assert np.array_equal(img[..., 3], ref[..., 3])
+    red = (ref[..., 0] == 255) & (ref[..., 1] == 0) & (ref[..., 2] == 0)
+    assert np.array_equal(red, (img[..., 0] == 255) & (img[..., 1] == 0) & (img[..., 2] == 0))
+    assert np.abs(img.astype(int) - ref.astype(int)).max() <= 1
+
+
+def test_lod_pressure_policy(trees):
+    """Decrease LOD when the cache is too small (the reference's todo): with
+    the policy on, frames whose session filled the cache coarsen the next
+    frame's voxel size until a frame fits; with it off the size never moves."""
+    w, h = 256, 256
+    m = _matrix(C1_CAMERA, w, h)
+    runs = {}
+    for on in (False, True):
+        ld, cm, rt = _scene(trees["terrain10"], 80, w, h)
+        rt.set_lod_pressure(on, max_lod_voxel_size=32.0, grow=2.0, shrink=1.25)
+        seq = []
+        for _ in range(10):
+            rt.RenderFrame(m)
+            st = rt.stats()
+            seq.append((st["lod_voxel_size"], st["session_filled"]))
+        runs[on] = seq
+    off, on = runs[False], runs[True]
+    assert all(l == 1.0 for l, _ in off)
+    assert off[0][1] == 1  # the cache is too small for this frame at voxel size 1
+    assert on[0] == off[0]
+    f32 = np.float32
+    for (l0, f0), (l1, _) in zip(on, on[1:]):  # grows after a filled session, never beyond the cap (float math)
+        assert f32(l1) == (min(f32(32.0), f32(l0) * f32(2.0)) if f0 else max(f32(1.0), f32(l0) / f32(1.25)))
+    assert any(f == 0 for _, f in on)  # a coarser frame fits in the cache

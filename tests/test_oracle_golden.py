@@ -88,3 +88,24 @@ def test_golden_inputs_regenerate(built):
     d = np.load(os.path.join(GOLDEN, "feedback_unique.npz"))
     np.testing.assert_array_equal(d["small_words"], feedback_words(5000, 5))
     np.testing.assert_array_equal(d["no_nohit_words"], feedback_words(3000, 8, no_hit=False))
+
+
+@pytest.mark.parametrize("name", sorted(__import__("tests.golden.common", fromlist=["DEPTH_CASES"]).DEPTH_CASES))
+def test_oracle_depth_view(trees, name):
+    """The oracle's restatement of raytracer.cl (the reference's debug depth
+    view) against the reference kernel run by the harness: red (fault or
+    error) and black (miss) pixels exact, grey within 1 LSB (log is the C
+    library's)."""
+    from oracle import oracle as O
+    from tests.golden.common import DEPTH_CASES
+    case = DEPTH_CASES[name]
+    d = np.load(os.path.join(GOLDEN, "depth_views.npz"))
+    w, h = case["size"]
+    sc = O.OracleScene(trees[case["tree"]], case["max_blocks"])
+    img = sc.depth_view(d[name + "_matrix"], case["lod"], w, h)
+    sc.close()
+    ref = d[name + "_image"]
+    assert np.array_equal(img[..., 3], ref[..., 3])
+    red = (ref[..., 0] == 255) & (ref[..., 1] == 0)
+    assert np.array_equal(red, (img[..., 0] == 255) & (img[..., 1] == 0))
+    assert np.abs(img.astype(int) - ref.astype(int)).max() <= 1
