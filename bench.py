@@ -76,6 +76,7 @@ def parse():
     ap.add_argument("--spheres", type=int, default=None, help="override the workload's sphere count")
     ap.add_argument("--cache-mib", type=int, default=None, help="override the workload's cache size")
     ap.add_argument("--depth", type=int, default=None, help="override the workload's octree depth")
+    ap.add_argument("--c2-log2n", type=int, default=28, help="c2: 2^k feedback words (profiling uses a smaller k)")
     a = ap.parse_args()
     if a.workload in WORKLOADS:
         if a.spheres is not None:
@@ -851,7 +852,7 @@ def bench_c2(args, rank, world, local):
     import torch
 
     import rayt_gb300 as R
-    n = 1 << 28
+    n = 1 << args.c2_log2n
     steps = args.steps or 20
     words = zipf_words(n)
     if args.impl == "reference":
@@ -866,7 +867,7 @@ def bench_c2(args, rank, world, local):
             k += 1
         el = (time.time() - t) / k
         v = sub.size / el / 1e9
-        return {"metric": "Gkeys/s feedback compaction+sort+unique (2^28 words)", "value": round(v, 4),
+        return {"metric": "Gkeys/s feedback compaction+sort+unique (2^%d words)" % args.c2_log2n, "value": round(v, 4),
                 "unit": "Gkeys/s", "impl": "reference", "n_gpus": 1, "steps": k, "warmup": 0,
                 "ms_per_step": round(el * 1e3, 3), "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "int32", "data": "synthetic",
@@ -906,16 +907,30 @@ def bench_c2(args, rank, world, local):
     peak, kind = hbm_peak()
     if rank != 0:
         return None
-    return {"metric": "Gkeys/s feedback compaction+sort+unique (2^28 words)",
+    traffic = profile_traffic("sort_c2")
+    # CPU baseline: the reference's merge sort + Hillis-Steele scan pipeline
+    # (oracle) on a 2^22-word sample of the same words
+    from oracle import oracle as O
+    sub = words[: 1 << 22]
+    t = time.time()
+    k = 0
+    while k < 1 or (time.time() - t < args.cpu_seconds and k < steps):
+        O.feedback_unique(sub, 4096)
+        k += 1
+    cpu = {"value": round(sub.size * k / (time.time() - t) / 1e9, 4), "unit": "Gkeys/s", "cores": os.cpu_count() or 1,
+           "kind": "port", "sample": "%d calls on 2^22 of the words (merge sort + Hillis-Steele scan)" % k}
+    return {"metric": "Gkeys/s feedback compaction+sort+unique (2^%d words)" % args.c2_log2n,
             "value": round(sum_over_ranks(n * steps, world) / t_dev / 1e9, 4), "unit": "Gkeys/s", "n_gpus": world,
             "steps": steps, "warmup": args.warmup, "ms_per_step": round(t_dev / steps * 1e3, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": {"workload": "c2", "n": n, "kept": m, "unique": cnt, "l2": "inputs (1 GiB) larger than L2"},
+            "config": {"workload": "c2", "n": n, "kept": m, "unique": cnt,
+                       "l2": "inputs (%d MiB) larger than L2" % (4 * n >> 20) if 4 * n > (129 << 20) else "inputs in L2"},
             "e2e": {"value": round(n * steps / t_e2e / 1e9, 4), "unit": "Gkeys/s", "h2d_bytes_per_step": 4 * n,
                     "d2h_bytes_per_step": 4 * cnt},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(achieved / peak, 4), "traffic": None, "peak_source": kind},
-            "cpu_baseline": None, "gpu_launches": steps * 7, "clocks": clk}
+                         "frac": round(achieved / peak, 4), "traffic": traffic if n == 1 << 28 else None,
+                         "peak_source": kind, "kernel": "compaction + 4 digit passes + unique (one call)"},
+            "cpu_baseline": cpu, "gpu_launches": steps * 7, "clocks": clk}
 
 
 def main():

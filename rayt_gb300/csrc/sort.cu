@@ -56,21 +56,36 @@ __device__ __forceinline__ unsigned long long lb_word(uint32_t tag, uint32_t fla
 }
 
 // Sum of the values published by tiles before `tile` for one lane of a
-// look-back table with `stride` words per tile.
+// look-back table with `stride` words per tile.  Predecessors are read
+// kLookAhead at a time (independent loads in flight together), then consumed
+// newest first until an inclusive prefix appears; a word not yet published is
+// polled (bounded) before the walk goes on.
+constexpr int kLookAhead = 4;
+__device__ __forceinline__ bool lb_ready(unsigned long long w, uint32_t tag) {
+  return (uint32_t)(w >> 34) == tag && ((w >> 32) & 3u) != 0;
+}
 __device__ uint32_t look_back(const unsigned long long* status, int tile, int stride, int lane, uint32_t tag) {
   uint32_t excl = 0;
-  for (int j = tile - 1; j >= 0; --j) {
-    unsigned long long w;
-    long long spins = 0;
-    while ((uint32_t)((w = ld_volatile64(status + (size_t)j * stride + lane)) >> 34) != tag ||
-           ((w >> 32) & 3u) == 0) {
-      if (++spins > kSpinLimit) {
-        atomicExch(&g_error_flag, 1);
-        return excl;
+  for (int j = tile - 1; j >= 0; j -= kLookAhead) {
+    const int k = min(kLookAhead, j + 1);
+    unsigned long long w[kLookAhead];
+#pragma unroll
+    for (int i = 0; i < kLookAhead; ++i)
+      if (i < k) w[i] = ld_volatile64(status + (size_t)(j - i) * stride + lane);
+#pragma unroll
+    for (int i = 0; i < kLookAhead; ++i) {
+      if (i >= k) break;
+      long long spins = 0;
+      while (!lb_ready(w[i], tag)) {
+        if (++spins > kSpinLimit) {
+          atomicExch(&g_error_flag, 1);
+          return excl;
+        }
+        w[i] = ld_volatile64(status + (size_t)(j - i) * stride + lane);
       }
+      excl += (uint32_t)w[i];
+      if (((w[i] >> 32) & 3u) == 2u) return excl;
     }
-    excl += (uint32_t)w;
-    if (((w >> 32) & 3u) == 2u) break;
   }
   return excl;
 }
@@ -244,7 +259,9 @@ __global__ void __launch_bounds__(kThreads, 4) digit_kernel(const uint32_t* in, 
       __syncwarp();
     }
     __syncthreads();
-    // per digit: exclusive prefix over warps, tile total, look-back
+    // per digit: exclusive prefix over warps and the tile's count; the count
+    // is published at once so later tiles' look-backs can pass this one
+    uint32_t tile_count;
     {
       const int d = threadIdx.x;
       uint32_t run = 0;
@@ -254,16 +271,8 @@ __global__ void __launch_bounds__(kThreads, 4) digit_kernel(const uint32_t* in, 
         s_warp[w][d] = run;
         run += v;
       }
-      unsigned long long* st = status + (size_t)tile * kBuckets + d;
-      if (tile == 0) {
-        st_volatile64(st, lb_word(tag, 2u, run));
-        s_global[d] = digit_base[d];
-      } else {
-        st_volatile64(st, lb_word(tag, 1u, run));
-        const uint32_t excl = look_back(status, tile, kBuckets, d, tag);
-        st_volatile64(st, lb_word(tag, 2u, excl + run));
-        s_global[d] = digit_base[d] + excl;
-      }
+      tile_count = run;
+      st_volatile64(status + (size_t)tile * kBuckets + d, lb_word(tag, tile == 0 ? 2u : 1u, run));
       s_tile_start[d] = run;  // temporarily the count; scanned below
     }
     __syncthreads();
@@ -281,13 +290,25 @@ __global__ void __launch_bounds__(kThreads, 4) digit_kernel(const uint32_t* in, 
       for (int k = 0; k < 8; ++k) { s_tile_start[lane * 8 + k] = run; run += v[k]; }
     }
     __syncthreads();
-    // stage keys in tile-local sorted order
+    // stage keys in tile-local sorted order (frees the key registers before the
+    // look-back)
 #pragma unroll
     for (int r = 0; r < kItems; ++r) {
       const int li = warp * (kItems * 32) + r * 32 + lane;
       if (li < valid) {
         const uint32_t d = (keys[r] >> shift) & 255u;
         s_keys[s_tile_start[d] + s_warp[warp][d] + ranks[r]] = keys[r];
+      }
+    }
+    // global position of each digit run: look-back over earlier tiles
+    {
+      const int d = threadIdx.x;
+      if (tile == 0) {
+        s_global[d] = digit_base[d];
+      } else {
+        const uint32_t excl = look_back(status, tile, kBuckets, d, tag);
+        st_volatile64(status + (size_t)tile * kBuckets + d, lb_word(tag, 2u, excl + tile_count));
+        s_global[d] = digit_base[d] + excl;
       }
     }
     __syncthreads();

@@ -1,5 +1,5 @@
-// Tracing pass, the hot path: a persistent, work-stealing traversal kernel
-// over the rays of one or many views.
+// Tracing passes, the hot path: traversal of the rays of one or many views
+// against the block cache, plus the reference's debug depth view.
 //
 // Per ray this fuses what the reference runs as separate full-frame kernels
 // with a 48-byte TracingState round trip through memory:
@@ -10,16 +10,25 @@
 //   final colour    FinishTracingFrame (rayt/GPU_renderer/kernels/finish_tracing_frame.cl:3-24)
 //   block words     NodeToBlockKernel  (rayt/GPU_renderer/kernels/feedback_compression.cl:4-13)
 //
-// Scheduling: one CTA per SM slot stays resident; every warp takes rays from a
-// global counter (first pass: 32-pixel tiles of all views, 8x4 by default,
-// lane i of a tile = pixel (i % tile_w, i / tile_w); later passes: the
-// compacted list of rays that faulted).  A warp advances its rays one CastRay iteration at a time and,
-// as soon as `refill` lanes are idle, hands those lanes the next rays, so
-// lanes do not sit out a warp's longest ray and the grid has no tail.
+// Kernels:
+//   trace_kernel             first pass, one thread per ray over the 32-pixel
+//                            tiles of all views of the launch (4x8 by default;
+//                            lane i of a tile = pixel (i % tile_w, i / tile_w))
+//   trace_queue_kernel       later passes: persistent warps take 32 rays at a
+//                            time of the compacted list of rays that faulted
+//   trace_persistent_kernel  first pass with work stealing: warps stop their
+//                            rays every step_budget iterations and refill idle
+//                            lanes (an autotuner candidate; slower on the
+//                            measured workloads, see the design notes)
+//   finish_kernel            FinishTracingFrame for rays still faulted
+//   depth_view_kernel        raytracer.cl, the reference's debug depth view
+//   unique_from_bits_kernel  the feedback bitmaps as the reference's sorted
+//                            unique array
 // A ray that ends (hit, miss, iteration limit) writes its final RGBA8 pixel;
 // a ray that faults on a missing block is appended with its state (advanced
-// origin, direction, parent node) to the next pass's list.  Feedback goes into
-// two bitmaps (fault blocks; hit cache blocks with the duplicate flag).
+// origin, direction, parent node, pixel) to the next pass's list.  Feedback
+// goes into two bitmaps (fault blocks; hit cache blocks with the duplicate
+// flag).
 //
 // FP32 arithmetic follows the reference's operation order exactly; the file is
 // compiled with --fmad=false and IEEE division/sqrt so no operation is fused or
