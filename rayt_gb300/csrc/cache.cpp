@@ -57,11 +57,17 @@ class Cache::ReadPool {
     cv_.notify_all();
   }
   // Runs fn(0..n-1) on the pool and the calling thread.
-  void Run(int n, const std::function<void(int)>& fn) {
-    if (n <= 0) return;
+  void Run(int n, std::function<void(int)> fn) {
+    Start(n, std::move(fn));
+    Wait();
+  }
+  // Hands fn(0..n-1) to the workers and returns at once; Wait() joins in and
+  // returns when every item is done.  One job at a time.
+  void Start(int n, std::function<void(int)> fn) {
     {
       std::lock_guard<std::mutex> lock(mu_);
-      fn_ = &fn;
+      job_ = std::move(fn);
+      fn_ = &job_;
       n_ = n;
       next_.store(0);
       done_ = 0;
@@ -69,7 +75,10 @@ class Cache::ReadPool {
       gen_seen_.store(gen_, std::memory_order_release);
     }
     cv_.notify_all();
-    const int mine = Work(fn, n);
+  }
+  void Wait() {
+    if (!fn_) return;
+    const int mine = Work(job_, n_);
     std::unique_lock<std::mutex> lock(mu_);
     done_ += mine;
     done_cv_.wait(lock, [this] { return done_ == n_ && active_ == 0; });
@@ -81,7 +90,8 @@ class Cache::ReadPool {
   std::vector<std::thread> workers_;
   std::mutex mu_;
   std::condition_variable cv_, done_cv_;
-  const std::function<void(int)>* fn_ = nullptr;
+  std::function<void(int)> job_;
+  const std::function<void(int)>* fn_ = nullptr;  // &job_ while a job runs
   int n_ = 0, done_ = 0, active_ = 0;
   uint64_t gen_ = 0;
   std::atomic<uint64_t> gen_seen_{0};  // gen_, readable without the lock
@@ -444,13 +454,24 @@ int Cache::ReadOne(int pos, int block) {
 
 // Reads blocks[0..n) into positions [staged_, staged_ + n) in parallel.
 int Cache::Prefetch(const int* blocks, int n) {
+  StartRead(blocks, n);
+  FinishRead();
+  return RAYT_OK;
+}
+
+// Starts reading blocks[0..n) into positions [staged_, staged_ + n) on the
+// pool and claims the positions; FinishRead() waits for them.  The caller
+// may place earlier positions meanwhile (reads touch only their positions).
+void Cache::StartRead(const int* blocks, int n) {
   const int first = staged_;
-  const auto t0 = std::chrono::steady_clock::now();
-  pool_->Run(n, [&](int i) { ReadOne(first + i, blocks[i]); });
-  stats_.io_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  read_started_ = std::chrono::steady_clock::now();
+  pool_->Start(n, [this, first, blocks](int i) { ReadOne(first + i, blocks[i]); });
   for (int i = 0; i < n; ++i) h_slots_[(size_t)stage_cap_ * half_ + first + i] = -1;
   staged_ += n;
-  return RAYT_OK;
+}
+void Cache::FinishRead() {
+  pool_->Wait();
+  stats_.io_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - read_started_).count();
 }
 
 // UploadBlock (gpu-octree-cache.cpp:102-234) for the block staged at `pos`;
@@ -598,22 +619,34 @@ int Cache::RequestBlock(int block) {
   return RAYT_OK;
 }
 // EndRequestTransaction (gpu-octree-cache-manager.cpp:150-194)
-// The pending blocks are read a chunk at a time in parallel (reads have no
-// side effects), then placed one by one in request order until the
-// transaction fills the cache, exactly as the reference's loop does.
+// The pending blocks are placed one by one in request order until the
+// transaction fills the cache, exactly as the reference's loop does.  Reads
+// have no side effects, so they run ahead: the pool reads the next chunk of
+// kReadChunk blocks while this thread places the current one.
 int Cache::EndTransaction() {
   if (!in_transaction_) return fail(RAYT_E_STATE, "no open transaction");
+  constexpr int kReadChunk = 64;
   int rc = RAYT_OK;
-  size_t i = 0;
+  size_t i = 0;          // next pending block to read
   bool filled = false;
-  while (rc == RAYT_OK && !filled && i < pending_.size()) {
-    if (TransactionFilled()) break;
-    if (staged_ == stage_cap_ && (rc = NextHalf()) != RAYT_OK) break;
-    const int n = (int)std::min<size_t>((size_t)(stage_cap_ - staged_), pending_.size() - i);
-    const int first = staged_;
-    if ((rc = Prefetch(pending_.data() + i, n)) != RAYT_OK) break;
+  int chunk_first = -1;  // staging position of the chunk being read, -1: none
+  int chunk_n = 0;
+  auto start_chunk = [&]() {
+    if (i >= pending_.size() || staged_ == stage_cap_) return;
+    const int n = (int)std::min<size_t>({(size_t)kReadChunk, (size_t)(stage_cap_ - staged_), pending_.size() - i});
+    chunk_first = staged_;
+    chunk_n = n;
+    StartRead(pending_.data() + i, n);
     i += n;
-    for (int k = 0; k < n; ++k) {
+  };
+  if (!pending_.empty() && staged_ == stage_cap_) rc = NextHalf();
+  if (rc == RAYT_OK && !TransactionFilled()) start_chunk();
+  while (rc == RAYT_OK && chunk_first >= 0) {
+    FinishRead();
+    const int first = chunk_first, n = chunk_n;
+    chunk_first = -1;
+    if (!filled && !TransactionFilled()) start_chunk();  // read ahead while placing
+    for (int k = 0; k < n && !filled; ++k) {
       if (TransactionFilled()) {
         filled = true;
         break;
@@ -621,7 +654,13 @@ int Cache::EndTransaction() {
       if (block_slot_[meta_[(size_t)stage_cap_ * half_ + first + k].block] >= 0) continue;
       if ((rc = Place(first + k, nullptr)) != RAYT_OK) break;
     }
+    if (rc != RAYT_OK || filled) break;
+    if (chunk_first < 0 && i < pending_.size()) {  // the half is full: continue in the other one
+      if ((rc = NextHalf()) != RAYT_OK) break;
+      start_chunk();
+    }
   }
+  if (chunk_first >= 0) FinishRead();  // a read-ahead the transaction no longer needs
   pending_.clear();
   const int frc = FlushTo(staged_);
   in_transaction_ = false;

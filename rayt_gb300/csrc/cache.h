@@ -2,6 +2,7 @@
 // device buffers and batched uploads).  See cache.cpp.
 #pragma once
 #include <cuda_runtime.h>
+#include <chrono>
 #include <cstdint>
 #include <string>
 #include <unordered_map>
@@ -121,6 +122,9 @@ class Cache {
 
   int ReadOne(int pos, int block);
   int Prefetch(const int* blocks, int n);
+  void StartRead(const int* blocks, int n);
+  void FinishRead();
+  std::chrono::steady_clock::time_point read_started_;
   int Place(int pos, std::vector<int>* queue);
   int Unload();
   void AddPatch(bool far_buffer, uint32_t index, uint32_t value);
