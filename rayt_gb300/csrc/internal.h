@@ -37,7 +37,19 @@ struct ViewDesc {
   int tile_base;           // first tile of this view in the launch's tile space
   float lod;               // lod_voxel_size
   int pix_base;            // first pixel of the view in the shared image buffer
+  float origin[4];         // InitTracingFrame's ray origin (m[2], m[6], m[10], 0) / m[14], per view
+  const float* coords;     // PixelCoords(width, height) in device memory
 };
+
+// InitTracingFrame's normalised pixel coordinates, which depend only on the
+// view's size: centres (x + 0.5) / W * 2 - 1 for x in [0, W), corners
+// x / W * 2 - 1 for x in [0, W], then the same for y.  Computed once on the
+// host with IEEE float arithmetic (the same operations and rounding as the
+// kernel would do per ray), so looking them up changes no bit.
+size_t pixel_coords_count(int w, int h);
+void pixel_coords(int w, int h, float* out);
+// The per-view origin the same way: (m[2], m[6], m[10], 0) / m[14].
+void view_origin(const float* m, float* origin);
 
 struct TraceParams {
   // cache (the reference's cache format)

@@ -70,6 +70,7 @@ class Renderer {
   std::vector<int> group_tiles_;    // first-pass tiles per launch group of kViewsPerLaunch views
   uchar4* d_images_ = nullptr;      // every view's image at its pix_base
   int32_t* d_dense_ = nullptr;      // recorded feedback words, same layout
+  float* d_coords_ = nullptr;       // every view's pixel_coords()
   RayList lists_[2];
   // [pass block 0][fault bits][hit bits][pass block 1]: pass k clears its own
   // block and the bitmaps with one memset and reads the other block's ray
@@ -127,6 +128,7 @@ Renderer::~Renderer() {
   if (s_) cudaStreamSynchronize(s_);
   DropGraphs();
   cudaFree(d_images_);
+  cudaFree(d_coords_);
   for (auto& l : lists_) {
     cudaFree(l.origin);
     cudaFree(l.dir);
@@ -183,6 +185,18 @@ int Renderer::Init(Cache* cache, int n_views, const int* widths, const int* heig
   RAYT_CUDA_TRY(cudaHostGetDevicePointer((void**)&d_unique_, h_unique_, 0));
   RAYT_CUDA_TRY(cudaHostGetDevicePointer((void**)&d_counts_, h_counts_, 0));
   for (auto& e : ev_) RAYT_CUDA_TRY(cudaEventCreate(&e));
+  // the views' normalised pixel coordinates (they depend only on the sizes)
+  std::vector<size_t> coord_at(n_views);
+  std::vector<float> coords;
+  for (int v = 0; v < n_views; ++v) {
+    coord_at[v] = coords.size();
+    coords.resize(coords.size() + pixel_coords_count(views_[v].width, views_[v].height));
+    pixel_coords(views_[v].width, views_[v].height, coords.data() + coord_at[v]);
+  }
+  if (cudaMalloc(&d_coords_, coords.size() * sizeof(float)) != cudaSuccess)
+    return fail(RAYT_E_OOM, "pixel coordinate table allocation failed");
+  RAYT_CUDA_TRY(cudaMemcpy(d_coords_, coords.data(), coords.size() * sizeof(float), cudaMemcpyHostToDevice));
+  for (int v = 0; v < n_views; ++v) views_[v].coords = d_coords_ + coord_at[v];
   RAYT_CUDA_TRY(cudaMemsetAsync(d_images_, 0, (size_t)padded * 4, s_));
   RAYT_CUDA_TRY(cudaMemsetAsync(d_state_, 0, (bit_words + 2 * kBlockInts) * 4, s_));
   RAYT_CUDA_TRY(cudaStreamSynchronize(s_));
@@ -200,6 +214,7 @@ int Renderer::SetViews(const float* m) {
     for (int v = g * kViewsPerLaunch; v < end; ++v) {
       ViewDesc& d = views_[v];
       std::memcpy(d.m, m + 16 * v, sizeof(d.m));
+      view_origin(d.m, d.origin);
       d.lod = lod_used;
       d.tiles_x = (d.width + tw - 1) / tw;
       d.tile_base = (int)std::min<int64_t>(tiles, INT32_MAX);

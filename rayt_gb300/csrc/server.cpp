@@ -68,6 +68,7 @@ class Server {
     int64_t pixels = 0;      // w * h rounded up to 64
     uint64_t in_flight = 0;  // request being rendered (0: none)
     uchar4* host = nullptr;  // pinned copy of the last finished frame (deliver_to_host)
+    float* coords = nullptr; // pixel_coords(w, h) in device memory
   };
   struct Request {
     uint64_t id;
@@ -167,8 +168,10 @@ Server::~Server() {
   cudaFree(d_state_);
   cudaFreeHost(h_unique_);
   cudaFreeHost(h_counts_);
-  for (auto& c : clients_)
+  for (auto& c : clients_) {
     if (c.host) cudaFreeHost(c.host);
+    cudaFree(c.coords);
+  }
 }
 
 // First fit in the framebuffer pool (ranges ordered by base).
@@ -204,6 +207,13 @@ int Server::AddClient(int w, int h, int* id) {
   if (cfg_.deliver_to_host && !c.host &&
       cudaHostAlloc(&c.host, (size_t)w * h * 4, cudaHostAllocDefault) != cudaSuccess)
     return fail(RAYT_E_OOM, "pinned host image allocation failed");
+  std::vector<float> coords(pixel_coords_count(w, h));
+  pixel_coords(w, h, coords.data());
+  cudaFree(c.coords);
+  c.coords = nullptr;
+  if (cudaMalloc(&c.coords, coords.size() * sizeof(float)) != cudaSuccess)
+    return fail(RAYT_E_OOM, "pixel coordinate table allocation failed");
+  RAYT_CUDA_TRY(cudaMemcpy(c.coords, coords.data(), coords.size() * sizeof(float), cudaMemcpyHostToDevice));
   c.live = true;
   c.w = w;
   c.h = h;
@@ -224,6 +234,8 @@ int Server::RemoveClient(int id) {
   clients_[id].live = false;
   if (clients_[id].host) cudaFreeHost(clients_[id].host);
   clients_[id].host = nullptr;
+  cudaFree(clients_[id].coords);
+  clients_[id].coords = nullptr;
   return RAYT_OK;
 }
 
@@ -335,6 +347,8 @@ int Server::Step(int* finished) {
       const Client& c = clients_[f.client];
       ViewDesc v{};
       std::memcpy(v.m, f.m, sizeof(v.m));
+      view_origin(v.m, v.origin);
+      v.coords = c.coords;
       v.width = c.w;
       v.height = c.h;
       v.lod = cfg_.lod_voxel_size;

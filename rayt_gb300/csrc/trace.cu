@@ -52,35 +52,46 @@ __device__ __forceinline__ float dot4(float ax, float ay, float az, float aw, fl
   return r;
 }
 
+// 0 / d as an IEEE division gives it: a zero with d's sign, NaN for a zero
+// or NaN d.
+__device__ __forceinline__ float zero_over(float d) {
+  return (d == 0.0f || d != d) ? __int_as_float(0x7fffffff) : copysignf(0.0f, d);
+}
+
 // mul(float16, float3) of init_tracing_frame.cl:3-9
 __device__ __forceinline__ void mul_point(const float* m, float x, float y, float z, float* o) {
   float d = dot4(x, y, z, 1.0f, m[12], m[13], m[14], m[15]);
   o[0] = __fdiv_rn(dot4(x, y, z, 1.0f, m[0], m[1], m[2], m[3]), d);
   o[1] = __fdiv_rn(dot4(x, y, z, 1.0f, m[4], m[5], m[6], m[7]), d);
   o[2] = __fdiv_rn(dot4(x, y, z, 1.0f, m[8], m[9], m[10], m[11]), d);
-  o[3] = __fdiv_rn(0.0f, d);
+  o[3] = zero_over(d);
 }
 
-// InitTracingFrame for pixel (x, y) of view v.
+// InitTracingFrame for pixel (x, y) of view v.  The view's origin and its
+// normalised pixel coordinates come precomputed (the same IEEE operations,
+// done once per view and per column/row instead of per ray).
 __device__ __forceinline__ void init_ray(const ViewDesc& v, int x, int y, float4& o, float4& d) {
   const float* m = v.m;
   const int W = v.width, H = v.height;
-  float ox = __fdiv_rn(m[2], m[14]), oy = __fdiv_rn(m[6], m[14]), oz = __fdiv_rn(m[10], m[14]);
-  float ow = __fdiv_rn(0.0f, m[14]);
+  const float* cx = v.coords;          // (x + 0.5) / W * 2 - 1
+  const float* ax = cx + W;            // x / W * 2 - 1, x in [0, W]
+  const float* cy = ax + W + 1;        // (y + 0.5) / H * 2 - 1
+  const float* ay = cy + H;            // y / H * 2 - 1, y in [0, H]
+  const float ox = v.origin[0], oy = v.origin[1], oz = v.origin[2], ow = v.origin[3];
   float q[4];
-  mul_point(m, __fdiv_rn(x + 0.5f, (float)W) * 2 - 1, __fdiv_rn(y + 0.5f, (float)H) * 2 - 1, 0.0f, q);
+  mul_point(m, __ldg(cx + x), __ldg(cy + y), 0.0f, q);
   float dx = q[0] - ox, dy = q[1] - oy, dz = q[2] - oz, dw = q[3] - ow;
   float len = __fsqrt_rn(dot4(dx, dy, dz, dw, dx, dy, dz, dw));
   dx = __fdiv_rn(dx, len);
   dy = __fdiv_rn(dy, len);
   dz = __fdiv_rn(dz, len);
   float p1[4], p2[4];
-  mul_point(m, __fdiv_rn((float)x, (float)W) * 2 - 1, __fdiv_rn((float)y, (float)H) * 2 - 1, 0.0f, p1);
-  mul_point(m, __fdiv_rn((float)(x + 1), (float)W) * 2 - 1, __fdiv_rn((float)(y + 1), (float)H) * 2 - 1, 0.0f, p2);
-  float ax = p1[0] - p2[0], ay = p1[1] - p2[1], az = p1[2] - p2[2], aw = p1[3] - p2[3];
-  float bx = ox - p1[0], by = oy - p1[1], bz = oz - p1[2], bw = ow - p1[3];
-  float dist12 = __fsqrt_rn(dot4(ax, ay, az, aw, ax, ay, az, aw));
-  float dist01 = __fsqrt_rn(dot4(bx, by, bz, bw, bx, by, bz, bw));
+  mul_point(m, __ldg(ax + x), __ldg(ay + y), 0.0f, p1);
+  mul_point(m, __ldg(ax + x + 1), __ldg(ay + y + 1), 0.0f, p2);
+  float bx = p1[0] - p2[0], by = p1[1] - p2[1], bz = p1[2] - p2[2], bw = p1[3] - p2[3];
+  float ex = ox - p1[0], ey = oy - p1[1], ez = oz - p1[2], ew = ow - p1[3];
+  float dist12 = __fsqrt_rn(dot4(bx, by, bz, bw, bx, by, bz, bw));
+  float dist01 = __fsqrt_rn(dot4(ex, ey, ez, ew, ex, ey, ez, ew));
   float coef = __fdiv_rn(v.lod * dist12, dist01);
   o = make_float4(ox, oy, oz, 0.0f);
   d = make_float4(dx, dy, dz, coef);

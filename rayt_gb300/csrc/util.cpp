@@ -51,3 +51,24 @@ extern "C" {
 const char* rayt_last_error(void) { return rayt::g_last_error.c_str(); }
 const char* rayt_version(void) { return "rayt_gb300 0.1 (sm_103a)"; }
 }
+
+namespace rayt {
+
+size_t pixel_coords_count(int w, int h) { return (size_t)w + (w + 1) + h + (h + 1); }
+
+void pixel_coords(int w, int h, float* out) {
+  const float W = (float)w, H = (float)h;
+  for (int x = 0; x < w; ++x) *out++ = (x + 0.5f) / W * 2 - 1;
+  for (int x = 0; x <= w; ++x) *out++ = (float)x / W * 2 - 1;
+  for (int y = 0; y < h; ++y) *out++ = (y + 0.5f) / H * 2 - 1;
+  for (int y = 0; y <= h; ++y) *out++ = (float)y / H * 2 - 1;
+}
+
+void view_origin(const float* m, float* origin) {
+  origin[0] = m[2] / m[14];
+  origin[1] = m[6] / m[14];
+  origin[2] = m[10] / m[14];
+  origin[3] = 0.0f / m[14];
+}
+
+}  // namespace rayt
