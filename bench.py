@@ -193,6 +193,19 @@ def hbm_peak():
         return HBM_FALLBACK_GBS, "fallback"
 
 
+class roofline_range:
+    """NVTX range "roofline" around the launches the roofline object times, so
+    an ncu capture can select exactly them (--nvtx --nvtx-include roofline/)."""
+
+    def __enter__(self):
+        import torch
+        torch.cuda.nvtx.range_push("roofline")
+
+    def __exit__(self, *exc):
+        import torch
+        torch.cuda.nvtx.range_pop()
+
+
 def profile_traffic(name):
     """DRAM bytes per launch of the traversal kernel from the committed ncu
     summary (profiles/<name>.md, line 'traffic_bytes_per_launch: N')."""
@@ -374,7 +387,8 @@ def bench_frames(args, rank, world, local):
     # roofline of the dominant kernel (first-pass traversal) on the last camera
     m_last = mats[args.warmup + steps - 1]
     fetch = rt.count_fetches(m_last)
-    pass_ms = rt.time_pass(m_last, 5)
+    with roofline_range():
+        pass_ms = rt.time_pass(m_last, 5)
     alg_bytes = 4 * fetch["link_fetches"] + 4 * fetch["far_fetches"] + 16 * fetch["rays"]
     achieved = alg_bytes / (pass_ms / 1e3) / 1e9
     peak, peak_kind = hbm_peak()
@@ -537,7 +551,8 @@ def bench_batched(args, rank, world, local):
 
     # roofline of the first pass over all views
     fetch = rt.count_fetches(mats[frames - 1])
-    pass_ms = rt.time_pass(mats[frames - 1], 3)
+    with roofline_range():
+        pass_ms = rt.time_pass(mats[frames - 1], 3)
     alg_bytes = 4 * fetch["link_fetches"] + 4 * fetch["far_fetches"] + 16 * fetch["rays"]
     achieved = alg_bytes / (pass_ms / 1e3) / 1e9
     peak, peak_kind = hbm_peak()
@@ -567,8 +582,8 @@ def bench_batched(args, rank, world, local):
                            "note": "same frames, one RenderFrame per view (wall clock)"},
         "frames": {"passes_per_frame": round(passes / steps, 3)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
-                     "kernel": "trace_kernel<first pass>, all 64 views", "launch_ms": round(pass_ms, 4),
+                     "frac": round(achieved / peak, 4), "traffic": profile_traffic("trace_kernel_c4"),
+                     "peak_source": peak_kind, "kernel": "trace_kernel<first pass>, all 64 views", "launch_ms": round(pass_ms, 4),
                      "bytes_per_ray": round(alg_bytes / fetch["rays"], 2)},
         "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clk}
 
@@ -781,7 +796,8 @@ def bench_served(args, rank, world, local):
     # roofline of the first pass on the largest client view
     big = max(range(nclients), key=lambda c: pixels[c])
     fetch = rts[big].count_fetches(cams[big][0])
-    pass_ms = rts[big].time_pass(cams[big][0], 3)
+    with roofline_range():
+        pass_ms = rts[big].time_pass(cams[big][0], 3)
     alg_bytes = 4 * fetch["link_fetches"] + 4 * fetch["far_fetches"] + 16 * fetch["rays"]
     achieved = alg_bytes / (pass_ms / 1e3) / 1e9
     peak, peak_kind = hbm_peak()
@@ -823,8 +839,8 @@ def bench_served(args, rank, world, local):
                   "open_loop": {"frames_s": round(len(lat_plain) / span_plain, 1), "p50_ms": pp50, "p99_ms": pp99,
                                 "served_requests": len(lat_plain)}},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
-                     "kernel": "trace_kernel<first pass>, %dx%d client view" % sizes[big],
+                     "frac": round(achieved / peak, 4), "traffic": profile_traffic("trace_kernel_c5"),
+                     "peak_source": peak_kind, "kernel": "trace_kernel<first pass>, %dx%d client view" % sizes[big],
                      "launch_ms": round(pass_ms, 4), "bytes_per_ray": round(alg_bytes / fetch["rays"], 2)},
         "cpu_baseline": cpu, "gpu_launches": int(st["kernel_launches"]), "clocks": clk}
 
