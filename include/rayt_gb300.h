@@ -120,7 +120,10 @@ int rayt_build_terrain(const char* path, const rayt_terrain_params* params, int 
 typedef struct rayt_cache rayt_cache;
 
 /* GPUOctreeCacheManager(max_blocks_count, loader, context); max_blocks <= 0 means
- * every block of the file.  The tree must outlive the cache. */
+ * every block of the file.  The tree must outlive the cache.  Renderers and
+ * servers may share a cache (one LRU, one CUDA stream), one at a time: like
+ * the reference's single-threaded frame loop, a cache is not used by two host
+ * threads at once (a server's scheduler thread counts as one). */
 int rayt_cache_create(rayt_tree* tree, int max_blocks, rayt_cache** out);
 void rayt_cache_destroy(rayt_cache* cache);
 /* GPUOctreeCacheManager::InitialFillCache (gpu-octree-cache-manager.cpp:60-108). */
