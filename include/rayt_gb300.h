@@ -364,6 +364,14 @@ int rayt_feedback_unique(const int32_t* device_words, int n, int nodes_in_block,
  * so order them on one stream or synchronise in between.  The first call on a
  * device looks up the array's address; make it before any stream capture.
  * Returns after the result is on the device and *unique_count is set. */
+/* No counterpart in the reference.  Failure detection self-test: every wait
+ * of a kernel on another CTA's result (the sort's look-back) gives up after a
+ * time limit (1 s), sets a device error flag and returns, and the call reports
+ * RAYT_E_TIMEOUT with the context still usable.  This runs one such wait on a
+ * word nothing ever publishes, with a limit of limit_s seconds, and returns
+ * RAYT_OK when the wait gave up and was reported as it must. */
+int rayt_selftest_bounded_wait(double limit_s, void* stream);
+
 #define RAYT_FEEDBACK_UNIQUE_NOALLOC_MAX_WORDS (1 << 21)
 int rayt_feedback_unique_noalloc(const int32_t* device_words, int n, int nodes_in_block,
                                  int32_t* device_unique, int* unique_count, void* stream);

@@ -157,6 +157,9 @@ size_t scan_scratch_bytes(int n);
 cudaError_t scan_i32_device(int32_t* data, int n, void* scratch, size_t scratch_bytes, cudaStream_t s);
 // Device error flag set by bounded waits that gave up (decoupled look-back).
 int* device_error_flag();
+// Runs one wait on a word nothing publishes, with a limit of limit_s seconds
+// (restored to 1 s after); the wait must give up and set the error flag.
+cudaError_t bounded_wait_probe(double limit_s, cudaStream_t s);
 
 // ---- block upload --------------------------------------------------------------
 constexpr int kMaxChannels = 8;

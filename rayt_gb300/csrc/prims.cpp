@@ -81,6 +81,16 @@ int rayt_scan_i32(int32_t* data, int n, void* stream) {
   return rayt::check_device_error(s);
 }
 
+int rayt_selftest_bounded_wait(double limit_s, void* stream) {
+  if (!(limit_s > 0) || limit_s > 10) return fail(RAYT_E_ARG, "rayt_selftest_bounded_wait: limit out of range (0, 10] s");
+  std::lock_guard<std::mutex> lock(rayt::g_mu);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  RAYT_CUDA_TRY(rayt::bounded_wait_probe(limit_s, s));
+  const int rc = rayt::check_device_error(s);
+  if (rc == RAYT_E_TIMEOUT) return RAYT_OK;  // the wait gave up as it must
+  return rc != RAYT_OK ? rc : fail(RAYT_E_STATE, "bounded wait did not give up");
+}
+
 int rayt_feedback_unique(const int32_t* words, int n, int nib, int32_t* unique, int* unique_count, void* stream) {
   if (n < 0 || !unique_count || (n > 0 && (!words || !unique)) || nib < 0)
     return fail(RAYT_E_ARG, "rayt_feedback_unique: bad arguments");

@@ -34,9 +34,22 @@ constexpr int kItems = 16;
 constexpr int kTile = kThreads * kItems;  // 4096 keys
 constexpr int kBuckets = 256;
 constexpr int kPasses = 4;
-constexpr long long kSpinLimit = 1ll << 26;
+constexpr long long kSpinLimit = 1ll << 26;  // polls, a backstop to the time limit
 
 __device__ int g_error_flag;
+// Time limit of every wait on another CTA's result (ns): a correct wait ends in
+// microseconds, so one that lasts this long sets g_error_flag and gives up.
+__device__ unsigned long long g_wait_ns = 1000000000ull;
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+// True once a wait that began at `start` has run out of polls or time.
+__device__ __forceinline__ bool wait_over(long long& spins, unsigned long long start) {
+  return ++spins > kSpinLimit || ((spins & 63) == 0 && global_ns() - start > g_wait_ns);
+}
 // Call counter of the sort/unique kernels.  Their look-back words carry the
 // tag epoch * 8 + pass, so words left by earlier calls never look published
 // and the look-back table needs no clearing between passes or calls.
@@ -76,8 +89,9 @@ __device__ uint32_t look_back(const unsigned long long* status, int tile, int st
     for (int i = 0; i < kLookAhead; ++i) {
       if (i >= k) break;
       long long spins = 0;
+      const unsigned long long start = lb_ready(w[i], tag) ? 0 : global_ns();
       while (!lb_ready(w[i], tag)) {
-        if (++spins > kSpinLimit) {
+        if (wait_over(spins, start)) {
           atomicExch(&g_error_flag, 1);
           return excl;
         }
@@ -439,8 +453,9 @@ __global__ void __launch_bounds__(kThreads) scan_kernel(int32_t* data, int n, un
       for (int j = tile - 1; j >= 0; --j) {
         unsigned long long s;
         long long spins = 0;
+        const unsigned long long start = global_ns();
         while (((s = ld_volatile64(status + j)) >> 32) == 0) {
-          if (++spins > kSpinLimit) { atomicExch(&g_error_flag, 1); break; }
+          if (wait_over(spins, start)) { atomicExch(&g_error_flag, 1); break; }
         }
         excl += (uint32_t)s;
         if ((s >> 32) == 2 || (s >> 32) == 0) break;
@@ -496,7 +511,29 @@ cudaError_t run_passes(SortScratchLayout& l, int n, uint32_t*& cur, uint32_t*& o
 
 int compact_grid(int n) { return std::min(grid_for(n), 152 * 8); }
 
+// Waits, as a look-back does, on a word that nothing publishes: the wait must
+// give up after g_wait_ns, set the error flag and return.
+__global__ void bounded_wait_probe_kernel(const unsigned long long* never) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) look_back(never, 1, 1, 0, 1u);
+}
+
 }  // namespace
+
+cudaError_t bounded_wait_probe(double limit_s, cudaStream_t s) {
+  const unsigned long long limit = (unsigned long long)(limit_s * 1e9), normal = 1000000000ull;
+  unsigned long long* never = nullptr;
+  cudaError_t e = cudaMalloc(&never, 2 * sizeof(unsigned long long));
+  if (e != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(never, 0, 2 * sizeof(unsigned long long), s)) == cudaSuccess &&
+      (e = cudaMemcpyToSymbolAsync(g_wait_ns, &limit, sizeof(limit), 0, cudaMemcpyHostToDevice, s)) == cudaSuccess) {
+    bounded_wait_probe_kernel<<<1, 32, 0, s>>>(never);
+    e = cudaGetLastError();
+  }
+  cudaError_t e2 = cudaMemcpyToSymbolAsync(g_wait_ns, &normal, sizeof(normal), 0, cudaMemcpyHostToDevice, s);
+  cudaError_t e3 = cudaStreamSynchronize(s);
+  cudaFree(never);
+  return e != cudaSuccess ? e : (e2 != cudaSuccess ? e2 : e3);
+}
 
 int* device_error_flag() {
   int* p = nullptr;

@@ -113,3 +113,17 @@ def test_node_to_block_division_edges(built, nib):
     hit = (conv > 0) & (conv != NO_HIT)
     conv[hit] = ((((conv[hit] >> 1) - 1) // nib + 1) << 1) | (conv[hit] & 1)
     np.testing.assert_array_equal(_unique(words, nib), np.unique(conv).astype(np.int32))
+
+
+def test_bounded_wait_gives_up_and_context_survives(built):
+    """Failure detection without a fault: a wait on a word nothing publishes
+    gives up after its time limit, the call reports it, and the next sort on
+    the same context is correct."""
+    import time
+    t = time.time()
+    assert R.lib().rayt_selftest_bounded_wait(0.02, None) == 0
+    assert time.time() - t < 5.0
+    a = np.random.default_rng(3).integers(-1000, 1000, size=100000).astype(np.int32)
+    x = dev(a)
+    R.GPUSort(x, a.size)
+    np.testing.assert_array_equal(host(x), np.sort(a))
