@@ -149,65 +149,117 @@ __device__ __forceinline__ uint32_t divide(uint32_t x, Divider v) {
   return v.m ? (uint32_t)__umul64hi((unsigned long long)x, v.m) : x;
 }
 
-// Tiles of 4096 words, grid-strided.  A tile's kept keys go to one contiguous
-// range claimed with a single atomicAdd (order inside the tile by warp, then
-// round); the four 8-bit digit histograms of the kept keys build up in shared
-// memory on the way.
-template <bool kCompact>
-__global__ void __launch_bounds__(kThreads) compact_kernel(const int32_t* words, int n, int nib, Divider div,
-                                                           uint32_t* keys, int* count, uint32_t* hist) {
+// Tiles of 4096 words, grid-strided over the resident CTAs.  A thread owns 16
+// words of a tile, read as four 16-byte loads when `words` is 16-byte aligned
+// (scalar loads otherwise, and for the last, partial tile).  The next tile's
+// loads are issued before the current tile is processed, so memory latency
+// overlaps the work.  The per-word loop only drops NO_HIT words: each warp
+// appends the words it keeps to its own 1024-word region of shared memory.
+// NodeToBlock, the key mapping and the four 8-bit digit histograms run when
+// the regions are flushed, on the kept words with every lane busy (at 10%
+// kept words, doing them per word cost three quarters of the instructions of
+// an issue-bound kernel).  The CTA flushes, claiming its output range with
+// one atomicAdd on `claim`, only when a region could not take another tile or
+// after its last tile; the regions go out coalesced.  Input words are read
+// once, with evict-first loads, so they do not push the compacted keys (read
+// again by the digit passes) out of L2.  Keys leave a warp in any order: only
+// sorted keys leave the sort.
+constexpr int kRegion = 1024;  // keys per warp region; a tile adds at most 512
+
+template <bool kVec>
+__device__ __forceinline__ void load_words(int32_t (&w)[kItems], const int32_t* words, uint32_t n, uint32_t first) {
+  // thread's words: first + r * 128 + j, r, j = 0..3
+  if (kVec && first + (kItems * 32 - 4 * (threadIdx.x & 31)) <= n) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int4 v = __ldcs(reinterpret_cast<const int4*>(words + first + r * 128));
+      w[4 * r] = v.x; w[4 * r + 1] = v.y; w[4 * r + 2] = v.z; w[4 * r + 3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const uint32_t i = first + r * 128 + j;
+        w[4 * r + j] = i < n ? __ldcs(words + i) : kNoHit;
+      }
+  }
+}
+
+template <bool kCompact, bool kVec>
+__global__ void __launch_bounds__(kThreads) compact_kernel(const int32_t* words, int n_words, int nib, Divider div,
+                                                           uint32_t* keys, int* claim, uint32_t* hist) {
   __shared__ uint32_t sh[kPasses][kBuckets];
-  __shared__ uint32_t s_warp[kWarps];
+  __shared__ uint32_t s_keys[kWarps * kRegion];
+  __shared__ uint32_t s_fill[2][kWarps];  // by tile parity: a warp may write the next tile's entry early
   __shared__ uint32_t s_base;
   for (int i = threadIdx.x; i < kPasses * kBuckets; i += kThreads) (&sh[0][0])[i] = 0;
+  const uint32_t n = (uint32_t)n_words;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned lt = (1u << lane) - 1;
-  for (int base = blockIdx.x * kTile; base < n; base += gridDim.x * kTile) {
-    // warp w owns words base + w*512 + r*32 + lane, r = 0..15
-    uint32_t key[kItems];
-    unsigned mask[kItems];
-    uint32_t mine = 0;
+  const uint32_t mine = warp * (kItems * 32) + lane * 4;  // offset of the thread's first word in a tile
+  uint32_t* region = s_keys + warp * kRegion;
+  const uint32_t stride = gridDim.x * kTile;  // tiles of n < 2^31 words: base + stride stays below 2^32
+  int32_t cur[kItems], nxt[kItems];
+  uint32_t base = blockIdx.x * kTile;
+  load_words<kVec>(cur, words, n, base + mine);
+  uint32_t fill = 0;  // keys in this warp's region
+  __syncthreads();    // histograms zeroed
+  for (int parity = 0; base < n; base += stride, parity ^= 1) {
+    const uint32_t next = base + stride;
+    load_words<kVec>(nxt, words, n, next + mine);
 #pragma unroll
-    for (int r = 0; r < kItems; ++r) {
-      const int i = base + warp * (kItems * 32) + r * 32 + lane;
-      int32_t w = i < n ? words[i] : kNoHit;
-      bool keep = i < n;
-      if (kCompact) {
-        keep = keep && w != kNoHit;
-        if (keep && w > 0 && nib > 0) w = (int32_t)(((divide((uint32_t)((w >> 1) - 1), div) + 1) << 1) | (w & 1));
-      }
-      key[r] = (uint32_t)w ^ 0x80000000u;
-      mask[r] = __ballot_sync(0xffffffffu, keep);
-      mine += __popc(mask[r]);
+    for (int q = 0; q < kItems; ++q) {
+      const bool keep = kCompact ? cur[q] != kNoHit  // words past the end were loaded as NO_HIT
+                                 : base + mine + (q >> 2) * 128 + (q & 3) < n;
+      const unsigned mask = __ballot_sync(0xffffffffu, keep);
+      if (keep) region[fill + __popc(mask & lt)] = (uint32_t)cur[q];
+      fill += __popc(mask);
     }
-    if (lane == 0) s_warp[warp] = mine;
+#pragma unroll
+    for (int q = 0; q < kItems; ++q) cur[q] = nxt[q];
+    if (lane == 0) s_fill[parity][warp] = fill;
     __syncthreads();
+    bool flush = next >= n;
+#pragma unroll
+    for (int k = 0; k < kWarps; ++k) flush = flush || s_fill[parity][k] > kRegion - kItems * 32;
+    if (!flush) continue;
     if (threadIdx.x == 0) {
-      uint32_t run = 0;
-      for (int w = 0; w < kWarps; ++w) {
-        const uint32_t v = s_warp[w];
-        s_warp[w] = run;
-        run += v;
-      }
-      s_base = kCompact ? (uint32_t)atomicAdd(count, (int)run) : (uint32_t)base;
+      uint32_t total = 0;
+      for (int k = 0; k < kWarps; ++k) total += s_fill[parity][k];
+      s_base = (uint32_t)atomicAdd(claim, (int)total);
     }
     __syncthreads();
-    uint32_t pos = s_base + s_warp[warp];
+    uint32_t out = s_base;
+    for (int k = 0; k < warp; ++k) out += s_fill[parity][k];
+    for (uint32_t j = lane; j < fill; j += 32) {
+      int32_t v = (int32_t)region[j];
+      if (kCompact && v > 0 && nib > 0) v = (int32_t)(((divide((uint32_t)((v >> 1) - 1), div) + 1) << 1) | (v & 1));
+      const uint32_t key = (uint32_t)v ^ 0x80000000u;
 #pragma unroll
-    for (int r = 0; r < kItems; ++r) {
-      if (mask[r] & (1u << lane)) {
-        keys[pos + __popc(mask[r] & lt)] = key[r];
-#pragma unroll
-        for (int p = 0; p < kPasses; ++p) atomicAdd(&sh[p][(key[r] >> (8 * p)) & 255u], 1u);
-      }
-      pos += __popc(mask[r]);
+      for (int p = 0; p < kPasses; ++p) atomicAdd(&sh[p][(key >> (8 * p)) & 255u], 1u);
+      keys[out + j] = key;
     }
-    __syncthreads();  // s_warp / s_base are reused by the next tile
+    fill = 0;
+    __syncthreads();  // s_base is reused by the next flush
   }
+  __syncthreads();
   for (int i = threadIdx.x; i < kPasses * kBuckets; i += kThreads) {
     const uint32_t v = (&sh[0][0])[i];
     if (v) atomicAdd(hist + i, v);
   }
+}
+
+// Compaction launch: 16-byte loads when `words` allows them.
+template <bool kCompact>
+cudaError_t launch_compact(int grid, const int32_t* words, int n, int nib, uint32_t* keys, int* claim,
+                           uint32_t* hist, cudaStream_t s) {
+  const Divider div = make_divider((uint32_t)nib);
+  if ((reinterpret_cast<uintptr_t>(words) & 15) == 0)
+    compact_kernel<kCompact, true><<<grid, kThreads, 0, s>>>(words, n, nib, div, keys, claim, hist);
+  else
+    compact_kernel<kCompact, false><<<grid, kThreads, 0, s>>>(words, n, nib, div, keys, claim, hist);
+  return cudaGetLastError();
 }
 
 // hist counts -> exclusive offsets (one CTA of 256 threads); opens a new epoch
@@ -234,12 +286,19 @@ __global__ void hist_offsets_kernel(uint32_t* hist) {
 
 // ---- one stable counting pass over 8 bits ------------------------------------
 // Persistent: each CTA claims tiles in order from tile_counter until the
-// compacted keys run out, so the grid is the resident CTAs, not the input size.
+// compacted keys (known only on the device) run out, so the grid is the
+// resident CTAs, not the input size.  A CTA claims its next tile when it
+// starts the current one and loads the next tile's keys as soon as the current
+// keys are ranked and parked in shared memory, so the load latency and the
+// claim overlap the current tile's prefix, look-back and write-out.  (A next
+// tile is always above its CTA's current one, so the lowest unfinished tile is
+// always some CTA's current tile and every look-back ends.)
 __global__ void __launch_bounds__(kThreads, 4) digit_kernel(const uint32_t* in, uint32_t* out, const int* count,
                                                          int shift, const uint32_t* digit_base,
                                                          unsigned long long* status, int* tile_counter, int pass,
                                                          bool last, int32_t* final_out) {
-  __shared__ uint32_t s_keys[kTile];
+  __shared__ uint32_t s_keys[kTile];             // the tile in tile-local sorted order
+  __shared__ uint32_t s_in[kTile];               // the tile as loaded
   __shared__ uint32_t s_warp[kWarps][kBuckets];
   __shared__ uint32_t s_tile_start[kBuckets];   // tile-local start of each digit run
   __shared__ uint32_t s_global[kBuckets];       // global position of each digit run
@@ -247,32 +306,45 @@ __global__ void __launch_bounds__(kThreads, 4) digit_kernel(const uint32_t* in, 
   const int m = *count;
   const uint32_t tag = g_epoch * 8u + (uint32_t)pass;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (;;) {
-    if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1);
-    for (int i = threadIdx.x; i < kWarps * kBuckets; i += kThreads) (&s_warp[0][0])[i] = 0;
-    __syncthreads();
-    const int tile = s_tile;
-    const int base = tile * kTile;
-    if (base >= m) return;
-    const int valid = min(kTile, m - base);
+  const int w0 = warp * (kItems * 32);  // warp `warp` ranks keys [w0, w0 + 512) of a tile, 32 per round
 
-    // warp `warp` ranks keys [warp*512, warp*512+512) of the tile, 32 per round
-    uint32_t keys[kItems];
-    uint32_t ranks[kItems];
+  if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1);
+  for (int i = threadIdx.x; i < kWarps * kBuckets; i += kThreads) (&s_warp[0][0])[i] = 0;
+  __syncthreads();
+  int tile = s_tile;
+  __syncthreads();  // every thread has read s_tile
+  if ((long long)tile * kTile >= m) return;
+  uint32_t keys[kItems];
+#pragma unroll
+  for (int r = 0; r < kItems; ++r) {
+    const int li = w0 + r * 32 + lane;
+    keys[r] = li < m - tile * kTile ? __ldg(in + tile * kTile + li) : 0u;
+  }
+  for (;;) {
+    const int base = tile * kTile;
+    const int valid = min(kTile, m - base);
+    if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1);  // the next tile
+
+    // ranking; the keys are already in registers, so the rounds' __syncwarp
+    // (which orders memory) holds up no loads
+    uint32_t ranks[kItems / 2];  // two 16-bit ranks (< 512) per word
 #pragma unroll
     for (int r = 0; r < kItems; ++r) {
-      const int li = warp * (kItems * 32) + r * 32 + lane;
+      const int li = w0 + r * 32 + lane;
       const bool ok = li < valid;
-      keys[r] = ok ? in[base + li] : 0u;
       const uint32_t d = ok ? (keys[r] >> shift) & 255u : 0x100u + (uint32_t)lane;  // invalid keys match nobody
       const unsigned peers = __match_any_sync(0xffffffffu, d);
       const uint32_t before = ok ? s_warp[warp][d] : 0u;
-      ranks[r] = before + __popc(peers & ((1u << lane) - 1));
+      const uint32_t rank = before + __popc(peers & ((1u << lane) - 1));
+      ranks[r / 2] = (r & 1) ? ranks[r / 2] | (rank << 16) : rank;
+      if (ok) s_in[li] = keys[r];  // parked in shared memory until the staging step
       __syncwarp();
       if (ok && lane == __ffs(peers) - 1) s_warp[warp][d] = before + __popc(peers);
       __syncwarp();
     }
     __syncthreads();
+    const int next = s_tile;
+    const long long next_base = (long long)next * kTile;
     // per digit: exclusive prefix over warps and the tile's count; the count
     // is published at once so later tiles' look-backs can pass this one
     uint32_t tile_count;
@@ -304,15 +376,22 @@ __global__ void __launch_bounds__(kThreads, 4) digit_kernel(const uint32_t* in, 
       for (int k = 0; k < 8; ++k) { s_tile_start[lane * 8 + k] = run; run += v[k]; }
     }
     __syncthreads();
-    // stage keys in tile-local sorted order (frees the key registers before the
-    // look-back)
+    // stage keys in tile-local sorted order, before the look-back
 #pragma unroll
     for (int r = 0; r < kItems; ++r) {
-      const int li = warp * (kItems * 32) + r * 32 + lane;
+      const int li = w0 + r * 32 + lane;
       if (li < valid) {
-        const uint32_t d = (keys[r] >> shift) & 255u;
-        s_keys[s_tile_start[d] + s_warp[warp][d] + ranks[r]] = keys[r];
+        const uint32_t k = s_in[li];
+        const uint32_t d = (k >> shift) & 255u;
+        const uint32_t rank = (r & 1) ? ranks[r / 2] >> 16 : ranks[r / 2] & 0xffffu;
+        s_keys[s_tile_start[d] + s_warp[warp][d] + rank] = k;
       }
+    }
+    // the next tile's keys are in flight during the look-back and write-out
+#pragma unroll
+    for (int r = 0; r < kItems; ++r) {
+      const long long gi = next_base + w0 + r * 32 + lane;
+      keys[r] = gi < m ? __ldg(in + gi) : 0u;
     }
     // global position of each digit run: look-back over earlier tiles
     {
@@ -326,7 +405,9 @@ __global__ void __launch_bounds__(kThreads, 4) digit_kernel(const uint32_t* in, 
       }
     }
     __syncthreads();
-    // contiguous write-out of each digit run
+    // contiguous write-out of each digit run; s_warp is cleared for the next
+    // tile on the way (the write-out does not read it)
+    for (int i = threadIdx.x; i < kWarps * kBuckets; i += kThreads) (&s_warp[0][0])[i] = 0;
     for (int i = threadIdx.x; i < valid; i += kThreads) {
       const uint32_t k = s_keys[i];
       const uint32_t d = (k >> shift) & 255u;
@@ -336,17 +417,23 @@ __global__ void __launch_bounds__(kThreads, 4) digit_kernel(const uint32_t* in, 
       else out[pos] = k;
     }
     __syncthreads();  // shared state is reused by the next tile
+    if (next_base >= m) return;
+    tile = next;
   }
 }
 
 // ---- unique of sorted keys -----------------------------------------------------
-// Persistent like digit_kernel; run starts counted per tile, prefix by look-back.
+// Persistent like digit_kernel, and pipelined the same way: a tile's run-start
+// keys are compacted into shared memory (each warp into its own range), the
+// next tile (claimed at the start of this one) is loaded, and only then does
+// the tile's look-back for its output position run.
 __global__ void __launch_bounds__(kThreads) unique_kernel(const uint32_t* keys, const int* count, int n_total,
                                                           int32_t* out, unsigned long long* status,
                                                           int* tile_counter, int* result) {
   __shared__ int s_tile;
   __shared__ uint32_t s_warp[kWarps];
   __shared__ uint32_t s_excl;
+  __shared__ uint32_t s_starts[kTile];
   const int m = *count;
   const uint32_t tag = g_epoch * 8u + 4u;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -358,33 +445,49 @@ __global__ void __launch_bounds__(kThreads) unique_kernel(const uint32_t* keys, 
     }
     return;
   }
+  // warp `warp` owns keys [w0, w0 + 512) of a tile, 32 per round (coalesced);
+  // a key starts a run when it differs from the key before it
+  const int w0 = warp * (kItems * 32);
+  const unsigned lt = (1u << lane) - 1;
+  if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1);
+  __syncthreads();
+  int tile = s_tile;
+  __syncthreads();  // every thread has read s_tile
+  if ((long long)tile * kTile >= m) return;
+  uint32_t k[kItems];
+  uint32_t prev_last = 0;  // the key before this warp's first key
+  {
+    const long long b = (long long)tile * kTile + w0;
+#pragma unroll
+    for (int r = 0; r < kItems; ++r) k[r] = b + r * 32 + lane < m ? __ldg(keys + b + r * 32 + lane) : 0u;
+    if (lane == 0 && b > 0 && b < m) prev_last = __ldg(keys + b - 1);
+  }
   for (;;) {
-    if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1);
-    __syncthreads();
-    const int tile = s_tile;
     const int base = tile * kTile;
-    if (base >= m) return;
     const int valid = min(kTile, m - base);
-    // thread t owns keys base + t*16 .. +15 (blocked)
-    uint32_t flags = 0, cnt = 0;
-    uint32_t k[kItems];
+    if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1);  // the next tile
+    uint32_t cnt = 0;
 #pragma unroll
     for (int r = 0; r < kItems; ++r) {
-      const int li = threadIdx.x * kItems + r;
-      if (li < valid) {
-        const int gi = base + li;
-        k[r] = keys[gi];
-        const bool start = gi == 0 || keys[gi - 1] != k[r];
-        if (start) { flags |= 1u << r; ++cnt; }
-      }
+      const int li = w0 + r * 32 + lane;
+      uint32_t prev = __shfl_up_sync(0xffffffffu, k[r], 1);
+      if (lane == 0) prev = prev_last;
+      prev_last = __shfl_sync(0xffffffffu, k[r], 31);
+      const bool start = li < valid && (base + li == 0 || prev != k[r]);
+      const unsigned starts = __ballot_sync(0xffffffffu, start);
+      if (start) s_starts[w0 + cnt + __popc(starts & lt)] = k[r];
+      cnt += __popc(starts);
     }
-    uint32_t incl = cnt;
-    for (int off = 1; off < 32; off <<= 1) {
-      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, off);
-      if (lane >= off) incl += t;
-    }
-    if (lane == 31) s_warp[warp] = incl;
+    if (lane == 0) s_warp[warp] = cnt;
     __syncthreads();
+    const int next = s_tile;
+    const long long next_base = (long long)next * kTile;
+    {  // the next tile's keys are in flight during the look-back and write-out
+      const long long b = next_base + w0;
+#pragma unroll
+      for (int r = 0; r < kItems; ++r) k[r] = b + r * 32 + lane < m ? __ldg(keys + b + r * 32 + lane) : 0u;
+      prev_last = lane == 0 && b > 0 && b < m ? __ldg(keys + b - 1) : 0u;
+    }
     if (threadIdx.x == 0) {
       uint32_t run = 0;
       for (int w = 0; w < kWarps; ++w) { const uint32_t v = s_warp[w]; s_warp[w] = run; run += v; }
@@ -405,11 +508,12 @@ __global__ void __launch_bounds__(kThreads) unique_kernel(const uint32_t* keys, 
       }
     }
     __syncthreads();
-    uint32_t pos = s_excl + s_warp[warp] + incl - cnt;
-#pragma unroll
-    for (int r = 0; r < kItems; ++r)
-      if ((flags & (1u << r)) && pos < (uint32_t)m) out[pos++] = (int32_t)(k[r] ^ 0x80000000u);
-    __syncthreads();  // s_tile / s_warp / s_excl are reused by the next tile
+    const uint32_t pos = s_excl + s_warp[warp];
+    for (uint32_t j = lane; j < cnt; j += 32)
+      if (pos + j < (uint32_t)m) out[pos + j] = (int32_t)(s_starts[w0 + j] ^ 0x80000000u);
+    __syncthreads();  // shared state is reused by the next tile
+    if (next_base >= m) return;
+    tile = next;
   }
 }
 
@@ -509,7 +613,18 @@ cudaError_t run_passes(SortScratchLayout& l, int n, uint32_t*& cur, uint32_t*& o
   return cudaSuccess;
 }
 
-int compact_grid(int n) { return std::min(grid_for(n), 152 * 8); }
+// One wave of resident compaction CTAs, at most the tiles of n words.
+int compact_grid(int n) {
+  static int resident = 0;
+  if (!resident) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, compact_kernel<true, true>, kThreads, 0);
+    resident = sms * (per_sm > 0 ? per_sm : 1);
+  }
+  return std::min(resident, grid_for(n));
+}
 
 // Waits, as a look-back does, on a word that nothing publishes: the wait must
 // give up after g_wait_ns, set the error flag and return.
@@ -554,9 +669,7 @@ cudaError_t feedback_unique_device(const int32_t* words, int n, int nib, int32_t
   if ((e = cudaMemsetAsync(l.tile_counter, 0, 16 * 4, s)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(l.count, 0, 4 * 4, s)) != cudaSuccess) return e;
   const int grid = compact_grid(n);
-  compact_kernel<true><<<grid, kThreads, 0, s>>>(words, n, nib, make_divider((uint32_t)nib), l.keys_a, l.count,
-                                                l.hist);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = launch_compact<true>(grid, words, n, nib, l.keys_a, l.count, l.hist, s)) != cudaSuccess) return e;
   uint32_t* cur = l.keys_a;
   uint32_t* other = l.keys_b;
   if ((e = run_passes(l, n, cur, other, nullptr, s)) != cudaSuccess) return e;
@@ -572,10 +685,10 @@ cudaError_t sort_i32_device(int32_t* data, int n, void* scratch, size_t scratch_
   cudaError_t e;
   if ((e = cudaMemsetAsync(l.hist, 0, kPasses * kBuckets * 4, s)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(l.tile_counter, 0, 16 * 4, s)) != cudaSuccess) return e;
-  if ((e = launch_fill_i32(l.count, n, 1, s)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(l.count, 0, 4 * 4, s)) != cudaSuccess) return e;
+  if ((e = launch_fill_i32(l.count, n, 1, s)) != cudaSuccess) return e;  // [0] keys; [2] the compaction's claims
   const int grid = compact_grid(n);
-  compact_kernel<false><<<grid, kThreads, 0, s>>>(data, n, 0, make_divider(1), l.keys_a, nullptr, l.hist);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = launch_compact<false>(grid, data, n, 0, l.keys_a, l.count + 2, l.hist, s)) != cudaSuccess) return e;
   uint32_t* cur = l.keys_a;
   uint32_t* other = l.keys_b;
   return run_passes(l, n, cur, other, data, s);

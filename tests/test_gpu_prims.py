@@ -99,6 +99,26 @@ def test_feedback_unique_large_properties(built, n):
     assert np.all(np.diff(u.astype(np.int64)) > 0) and u[-1] == NO_HIT
 
 
+@pytest.mark.parametrize("offset", [1, 2, 3])
+def test_unaligned_inputs(built, offset):
+    """Input arrays that start off a 16-byte boundary take the scalar-load
+    compaction; results equal the aligned ones."""
+    import torch
+    n = 3 * 4096 + 777
+    words = feedback_words(n, 5)
+    pad = dev(np.concatenate([np.zeros(offset, np.int32), words]))
+    out = torch.zeros(n, dtype=torch.int32, device="cuda")
+    cnt = R.feedback_unique(pad[offset:], n, 4096, out)
+    np.testing.assert_array_equal(host(out)[:cnt], _unique(words, 4096))
+    rng = np.random.default_rng(offset)
+    a = rng.integers(-2**31, 2**31 - 1, size=n, dtype=np.int64).astype(np.int32)
+    x = dev(np.concatenate([np.full(offset, 7, np.int32), a]))
+    R.GPUSort(x[offset:], n)
+    got = host(x)
+    np.testing.assert_array_equal(got[offset:], np.sort(a))
+    assert np.all(got[:offset] == 7)
+
+
 @pytest.mark.parametrize("nib", [1, 2, 3, 7, 1000, 1024, 4096, 8192, 10000, 65535, 65536])
 def test_node_to_block_division_edges(built, nib):
     """NodeToBlock divides node indices by nodes_in_block with a multiply-high;
