@@ -347,9 +347,11 @@ int rayt_scan_i32(int32_t* device_data, int n, void* stream);
  * NodeToBlock (when nodes_in_block > 0), then the sorted unique values
  * (signed ascending, RAYT_NO_HIT last when present) into device_unique (n
  * entries of room); *unique_count (host) receives the count.  Computed as
- * stream compaction -> LSD radix sort -> unique; the scratch memory is a
- * device buffer the library keeps per device and grows on demand.
- * device_words is not modified. */
+ * stream compaction, then, when the kept values span at most 32 per input
+ * word and at most 2^26, a bitmap over their range read in order; otherwise
+ * an LSD radix sort and unique.  The scratch memory is a device buffer the
+ * library keeps per device and grows on demand.  device_words is not
+ * modified. */
 int rayt_feedback_unique(const int32_t* device_words, int n, int nodes_in_block,
                          int32_t* device_unique, int* unique_count, void* stream);
 
@@ -364,6 +366,10 @@ int rayt_feedback_unique(const int32_t* device_words, int n, int nodes_in_block,
  * so order them on one stream or synchronise in between.  The first call on a
  * device looks up the array's address; make it before any stream capture.
  * Returns after the result is on the device and *unique_count is set. */
+#define RAYT_FEEDBACK_UNIQUE_NOALLOC_MAX_WORDS (1 << 21)
+int rayt_feedback_unique_noalloc(const int32_t* device_words, int n, int nodes_in_block,
+                                 int32_t* device_unique, int* unique_count, void* stream);
+
 /* No counterpart in the reference.  Failure detection self-test: every wait
  * of a kernel on another CTA's result (the sort's look-back) gives up after a
  * time limit (1 s), sets a device error flag and returns, and the call reports
@@ -371,10 +377,6 @@ int rayt_feedback_unique(const int32_t* device_words, int n, int nodes_in_block,
  * word nothing ever publishes, with a limit of limit_s seconds, and returns
  * RAYT_OK when the wait gave up and was reported as it must. */
 int rayt_selftest_bounded_wait(double limit_s, void* stream);
-
-#define RAYT_FEEDBACK_UNIQUE_NOALLOC_MAX_WORDS (1 << 21)
-int rayt_feedback_unique_noalloc(const int32_t* device_words, int n, int nodes_in_block,
-                                 int32_t* device_unique, int* unique_count, void* stream);
 
 #ifdef __cplusplus
 }

@@ -7,20 +7,27 @@
 // (rayt/GPU algorithms/kernels/scan.cl:2-12) and a scatter
 // (rayt/GPU_renderer/kernels/feedback_compression.cl:4-34).  Here:
 //   compact_kernel   drops NO_HIT words, applies NodeToBlock, maps each word
-//                    to an unsigned key (x ^ 0x80000000 keeps signed order) and
-//                    builds all four 8-bit digit histograms in the same read;
-//                    one atomicAdd per 4096-word tile claims its output range,
-//   digit_kernel     one stable counting pass per digit: tiles of 4096 keys,
-//                    warp match_any ranking, per-digit decoupled look-back for
-//                    the tile's global offsets, scatter staged through shared
-//                    memory so each digit run is written contiguously,
-//   unique_kernel    run starts counted per tile with a look-back prefix.
-// digit_kernel and unique_kernel are persistent: the resident CTAs claim tile
-// ids in order from an atomic counter until the compacted keys (known only on
-// the device) run out, so a tile only waits on tiles claimed by running CTAs.
-// Look-back words are tagged with a per-call epoch and the pass, so the table
-// is never cleared.  Every wait is bounded and sets an error flag instead of
-// hanging.
+//                    to an unsigned key (x ^ 0x80000000 keeps signed order),
+//                    builds all four 8-bit digit histograms and the key range
+//                    in the same read,
+//   hist_offsets     digit offsets; for feedback unique, chooses the path:
+//   bitmap path      (the keys span at most 32 values per input word and at
+//                    most 2^26) a bitmap over [min, max], whose set bits read
+//                    in order are the sorted unique set: range_hist and
+//                    range_partition split the keys into 256 ranges
+//                    (unstable), bucket_bitmap builds each range's slice of the
+//                    bitmap in shared memory (so frequent keys cost no global
+//                    atomics), bitmap_unique writes the set bits in order,
+//   radix path       (wider ranges, and GPUSort) four stable digit_kernel
+//                    passes (tiles of 4096 keys, warp match_any ranking,
+//                    per-digit decoupled look-back, scatter staged through
+//                    shared memory) and unique_kernel (run starts counted per
+//                    tile with a look-back prefix).
+// The kernels of the path not taken return at once.  The persistent kernels
+// claim tile ids in order from an atomic counter until the device-side count
+// runs out, so a tile only waits on tiles claimed by running CTAs.  Look-back
+// words are tagged with a per-call epoch and the pass, so the table is never
+// cleared.  Every wait is bounded and sets an error flag instead of hanging.
 #include <algorithm>
 
 #include "internal.h"
@@ -34,6 +41,17 @@ constexpr int kItems = 16;
 constexpr int kTile = kThreads * kItems;  // 4096 keys
 constexpr int kBuckets = 256;
 constexpr int kPasses = 4;
+// histogram rows: the four digits, then the range buckets' counts and offsets
+constexpr int kHistRows = kPasses + 2;
+constexpr int kRangeCounts = kPasses * kBuckets, kRangeOffsets = (kPasses + 1) * kBuckets;
+// the range partition's per-bucket cursors, one per 128-byte line: every tile
+// claims from most of them, and cursors sharing a line would share one L2 slice
+constexpr int kCursorStride = 32;
+// tile counters: digit passes 0-3, unique, bitmap unique, range histogram done
+// count, bucket items
+constexpr int kCtrUnique = 4, kCtrBitmapUnique = 5, kCtrRangeDone = 6, kCtrBuckets = 7;
+// the bitmap path keeps one range bucket's bitmap (span / 256 bits) in shared memory
+constexpr int kMaxSpanLog2 = 26;
 constexpr long long kSpinLimit = 1ll << 26;  // polls, a backstop to the time limit
 
 __device__ int g_error_flag;
@@ -104,6 +122,75 @@ __device__ uint32_t look_back(const unsigned long long* status, int tile, int st
   return excl;
 }
 
+// Sum of the values published by tiles before `tile` in a table of one word
+// per tile, looked back by a whole warp: lane i reads tile j - i, so one round
+// trip covers 32 predecessors.  The ready prefix of lanes up to the first
+// inclusive prefix is summed; a round that meets an unpublished word first
+// consumes the ready lanes before it and polls again (bounded).  All 32 lanes
+// call it and get the same result.
+__device__ uint32_t warp_look_back(const unsigned long long* status, int tile, uint32_t tag) {
+  const int lane = threadIdx.x & 31;
+  uint32_t excl = 0;
+  int j = tile - 1;
+  long long spins = 0;
+  unsigned long long start = 0;
+  while (j >= 0) {
+    const int t = j - lane;
+    const unsigned long long w = t >= 0 ? ld_volatile64(status + t) : 0ull;
+    const bool ready = t < 0 || lb_ready(w, tag);
+    const bool incl = t < 0 || (ready && ((w >> 32) & 3u) == 2u);
+    const unsigned not_ready = __ballot_sync(0xffffffffu, !ready);
+    const unsigned incl_mask = __ballot_sync(0xffffffffu, incl);
+    const int first_nr = not_ready ? __ffs(not_ready) - 1 : 32;
+    const int first_incl = incl_mask ? __ffs(incl_mask) - 1 : 32;
+    const int take = first_nr <= first_incl ? first_nr : first_incl + 1;  // lanes consumed this round
+    uint32_t v = lane < take && t >= 0 ? (uint32_t)w : 0u;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    excl += v;
+    if (first_incl < first_nr) return excl;  // reached an inclusive prefix (or the first tile)
+    j -= take;
+    if (take == 0) {  // the nearest unpublished word: poll it
+      if (start == 0) start = global_ns();
+      if (wait_over(spins, start)) {
+        if (lane == 0) atomicExch(&g_error_flag, 1);
+        return excl;
+      }
+    } else {
+      spins = 0;
+      start = 0;
+    }
+  }
+  return excl;
+}
+
+// Called by one warp: turns the per-warp counts s_warp[0..kWarps) into
+// exclusive offsets (s_warp[kWarps] = the tile's total), publishes the tile's
+// aggregate, looks back, publishes the inclusive prefix and returns the
+// tile's exclusive prefix.
+__device__ uint32_t tile_prefix(uint32_t* s_warp, unsigned long long* status, int tile, uint32_t tag) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t c = lane < kWarps ? s_warp[lane] : 0u;
+  uint32_t incl = c;
+  for (int off = 1; off < 32; off <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += t;
+  }
+  const uint32_t run = __shfl_sync(0xffffffffu, incl, 31);
+  __syncwarp();
+  if (lane < kWarps) s_warp[lane] = incl - c;
+  if (lane == 0) s_warp[kWarps] = run;
+  unsigned long long* st = status + tile;
+  if (tile == 0) {
+    if (lane == 0) st_volatile64(st, lb_word(tag, 2u, run));
+    return 0;
+  }
+  if (lane == 0) st_volatile64(st, lb_word(tag, 1u, run));
+  const uint32_t excl = warp_look_back(status, tile, tag);
+  if (lane == 0) st_volatile64(st, lb_word(tag, 2u, excl + run));
+  return excl;
+}
+
 struct SortScratchLayout {
   uint32_t* keys_a;
   uint32_t* keys_b;
@@ -111,6 +198,10 @@ struct SortScratchLayout {
   unsigned long long* status;     // tiles * kBuckets tagged look-back words
   int* tile_counter;              // kPasses + 2 counters
   int* count;                     // [0] compacted keys, [1] unique count
+  uint32_t* cursors;              // kBuckets range-partition cursors, kCursorStride words apart
+  uint32_t* range;                // [0] max of ~key, [1] max key, [2] path (kBitmapPath), [3] bitmap words,
+                                  // [4] range-bucket shift
+  size_t bitmap_bits;             // unique-by-bitmap capacity: the bitmap lives in keys_b
   size_t bytes;
 };
 
@@ -122,10 +213,13 @@ SortScratchLayout layout(void* base, int n) {
   uint8_t* b = static_cast<uint8_t*>(base);
   l.keys_a = reinterpret_cast<uint32_t*>(b + off); off += up((size_t)n * 4 + 16);
   l.keys_b = reinterpret_cast<uint32_t*>(b + off); off += up((size_t)n * 4 + 16);
-  l.hist = reinterpret_cast<uint32_t*>(b + off); off += up(kPasses * kBuckets * 4);
+  l.hist = reinterpret_cast<uint32_t*>(b + off); off += up(kHistRows * kBuckets * 4);
   l.status = reinterpret_cast<unsigned long long*>(b + off); off += up(tiles * kBuckets * 8);
   l.tile_counter = reinterpret_cast<int*>(b + off); off += up(16 * 4);
   l.count = reinterpret_cast<int*>(b + off); off += up(4 * 4);
+  l.range = reinterpret_cast<uint32_t*>(b + off); off += up(8 * 4);
+  l.cursors = reinterpret_cast<uint32_t*>(b + off); off += up(kBuckets * kCursorStride * 4);
+  l.bitmap_bits = (((size_t)n * 4 + 16) / 16) * 16 * 8;  // whole 16-byte units of keys_b
   l.bytes = off;
   return l;
 }
@@ -188,12 +282,16 @@ __device__ __forceinline__ void load_words(int32_t (&w)[kItems], const int32_t* 
 
 template <bool kCompact, bool kVec>
 __global__ void __launch_bounds__(kThreads) compact_kernel(const int32_t* words, int n_words, int nib, Divider div,
-                                                           uint32_t* keys, int* claim, uint32_t* hist) {
+                                                           uint32_t* keys, int* claim, uint32_t* hist,
+                                                           uint32_t* range) {
   __shared__ uint32_t sh[kPasses][kBuckets];
+  __shared__ uint32_t s_range[2];  // max of ~key (so the minimum), max key
   __shared__ uint32_t s_keys[kWarps * kRegion];
   __shared__ uint32_t s_fill[2][kWarps];  // by tile parity: a warp may write the next tile's entry early
   __shared__ uint32_t s_base;
   for (int i = threadIdx.x; i < kPasses * kBuckets; i += kThreads) (&sh[0][0])[i] = 0;
+  if (threadIdx.x < 2) s_range[threadIdx.x] = 0;
+  uint32_t not_min = 0, max_key = 0;
   const uint32_t n = (uint32_t)n_words;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned lt = (1u << lane) - 1;
@@ -238,48 +336,75 @@ __global__ void __launch_bounds__(kThreads) compact_kernel(const int32_t* words,
       const uint32_t key = (uint32_t)v ^ 0x80000000u;
 #pragma unroll
       for (int p = 0; p < kPasses; ++p) atomicAdd(&sh[p][(key >> (8 * p)) & 255u], 1u);
+      not_min = max(not_min, ~key);
+      max_key = max(max_key, key);
       keys[out + j] = key;
     }
     fill = 0;
     __syncthreads();  // s_base is reused by the next flush
+  }
+  if (range) {
+    not_min = __reduce_max_sync(0xffffffffu, not_min);
+    max_key = __reduce_max_sync(0xffffffffu, max_key);
+    if (lane == 0) {
+      atomicMax(&s_range[0], not_min);
+      atomicMax(&s_range[1], max_key);
+    }
   }
   __syncthreads();
   for (int i = threadIdx.x; i < kPasses * kBuckets; i += kThreads) {
     const uint32_t v = (&sh[0][0])[i];
     if (v) atomicAdd(hist + i, v);
   }
+  if (range && threadIdx.x < 2 && s_range[threadIdx.x]) atomicMax(range + threadIdx.x, s_range[threadIdx.x]);
 }
 
 // Compaction launch: 16-byte loads when `words` allows them.
 template <bool kCompact>
 cudaError_t launch_compact(int grid, const int32_t* words, int n, int nib, uint32_t* keys, int* claim,
-                           uint32_t* hist, cudaStream_t s) {
+                           uint32_t* hist, uint32_t* range, cudaStream_t s) {
   const Divider div = make_divider((uint32_t)nib);
   if ((reinterpret_cast<uintptr_t>(words) & 15) == 0)
-    compact_kernel<kCompact, true><<<grid, kThreads, 0, s>>>(words, n, nib, div, keys, claim, hist);
+    compact_kernel<kCompact, true><<<grid, kThreads, 0, s>>>(words, n, nib, div, keys, claim, hist, range);
   else
-    compact_kernel<kCompact, false><<<grid, kThreads, 0, s>>>(words, n, nib, div, keys, claim, hist);
+    compact_kernel<kCompact, false><<<grid, kThreads, 0, s>>>(words, n, nib, div, keys, claim, hist, range);
   return cudaGetLastError();
 }
 
+// Unique-by-bitmap: when the kept keys span at most `bitmap_bits` values (and
+// at most 2^26), a bitmap over [min, max] read in order is the sorted unique
+// set, and the radix passes are skipped.  range[2] holds the choice.
+constexpr uint32_t kBitmapPath = 1;
+
 // hist counts -> exclusive offsets (one CTA of 256 threads); opens a new epoch
-// for the look-back words of this call
-__global__ void hist_offsets_kernel(uint32_t* hist) {
-  __shared__ uint32_t s[kBuckets];
-  for (int p = 0; p < kPasses; ++p) {
-    s[threadIdx.x] = hist[p * kBuckets + threadIdx.x];
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      uint32_t run = 0;
-      for (int d = 0; d < kBuckets; ++d) {
-        const uint32_t v = s[d];
-        s[d] = run;
-        run += v;
-      }
+// for the look-back words of this call.  With `range`, also chooses between
+// the radix passes and the bitmap.
+__global__ void hist_offsets_kernel(uint32_t* hist, const int* count, uint32_t* range,
+                                    unsigned long long bitmap_bits) {
+  if (range && threadIdx.x == 0) {
+    const int m = *count;
+    const unsigned long long span = (unsigned long long)range[1] - (unsigned long long)(~range[0]) + 1ull;
+    const bool bitmap = m > 0 && span <= bitmap_bits && span <= (1ull << kMaxSpanLog2);
+    range[2] = bitmap ? kBitmapPath : 0u;
+    range[3] = bitmap ? (uint32_t)((span + 31) / 32) : 0u;
+    const int bits = span > 1 ? 64 - __clzll((long long)(span - 1)) : 0;  // bits of the largest key - min
+    range[4] = bits > 8 ? (uint32_t)(bits - 8) : 0u;
+  }
+  // warp p scans digit row p: 8 counts per lane, then a warp scan
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp < kPasses) {
+    uint32_t* row = hist + warp * kBuckets;
+    uint32_t v[8], sum = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) { v[k] = row[lane * 8 + k]; sum += v[k]; }
+    uint32_t incl = sum;
+    for (int off = 1; off < 32; off <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, off);
+      if (lane >= off) incl += t;
     }
-    __syncthreads();
-    hist[p * kBuckets + threadIdx.x] = s[threadIdx.x];
-    __syncthreads();
+    uint32_t run = incl - sum;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) { row[lane * 8 + k] = run; run += v[k]; }
   }
   if (threadIdx.x == 0) g_epoch = (g_epoch + 1) & ((1u << 27) - 1);
 }
@@ -293,16 +418,18 @@ __global__ void hist_offsets_kernel(uint32_t* hist) {
 // claim overlap the current tile's prefix, look-back and write-out.  (A next
 // tile is always above its CTA's current one, so the lowest unfinished tile is
 // always some CTA's current tile and every look-back ends.)
+// With `range` (feedback unique), skipped on the bitmap path.
 __global__ void __launch_bounds__(kThreads, 4) digit_kernel(const uint32_t* in, uint32_t* out, const int* count,
                                                          int shift, const uint32_t* digit_base,
                                                          unsigned long long* status, int* tile_counter, int pass,
-                                                         bool last, int32_t* final_out) {
+                                                         bool last, int32_t* final_out, const uint32_t* range) {
   __shared__ uint32_t s_keys[kTile];             // the tile in tile-local sorted order
   __shared__ uint32_t s_in[kTile];               // the tile as loaded
   __shared__ uint32_t s_warp[kWarps][kBuckets];
   __shared__ uint32_t s_tile_start[kBuckets];   // tile-local start of each digit run
   __shared__ uint32_t s_global[kBuckets];       // global position of each digit run
   __shared__ int s_tile;
+  if (range && range[2] == kBitmapPath) return;
   const int m = *count;
   const uint32_t tag = g_epoch * 8u + (uint32_t)pass;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -429,11 +556,12 @@ __global__ void __launch_bounds__(kThreads, 4) digit_kernel(const uint32_t* in, 
 // the tile's look-back for its output position run.
 __global__ void __launch_bounds__(kThreads) unique_kernel(const uint32_t* keys, const int* count, int n_total,
                                                           int32_t* out, unsigned long long* status,
-                                                          int* tile_counter, int* result) {
+                                                          int* tile_counter, int* result, const uint32_t* range) {
   __shared__ int s_tile;
-  __shared__ uint32_t s_warp[kWarps];
+  __shared__ uint32_t s_warp[kWarps + 1];
   __shared__ uint32_t s_excl;
   __shared__ uint32_t s_starts[kTile];
+  if (range[2] == kBitmapPath) return;
   const int m = *count;
   const uint32_t tag = g_epoch * 8u + 4u;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -488,24 +616,14 @@ __global__ void __launch_bounds__(kThreads) unique_kernel(const uint32_t* keys, 
       for (int r = 0; r < kItems; ++r) k[r] = b + r * 32 + lane < m ? __ldg(keys + b + r * 32 + lane) : 0u;
       prev_last = lane == 0 && b > 0 && b < m ? __ldg(keys + b - 1) : 0u;
     }
-    if (threadIdx.x == 0) {
-      uint32_t run = 0;
-      for (int w = 0; w < kWarps; ++w) { const uint32_t v = s_warp[w]; s_warp[w] = run; run += v; }
-      unsigned long long* st = status + tile;
-      if (tile == 0) {
-        st_volatile64(st, lb_word(tag, 2u, run));
-        s_excl = 0;
-      } else {
-        st_volatile64(st, lb_word(tag, 1u, run));
-        const uint32_t excl = look_back(status, tile, 1, 0, tag);
-        st_volatile64(st, lb_word(tag, 2u, excl + run));
-        s_excl = excl;
-      }
-      if (base + valid == m) {  // last tile: totals and the NO_HIT sentinel
-        int u = min((int)(s_excl + run), m);
+    if (warp == 0) {
+      const uint32_t excl = tile_prefix(s_warp, status, tile, tag);
+      if (lane == 0 && base + valid == m) {  // last tile: totals and the NO_HIT sentinel
+        int u = min((int)(excl + s_warp[kWarps]), m);
         if (m < n_total) out[u++] = kNoHit;
         *result = u;
       }
+      if (lane == 0) s_excl = excl;
     }
     __syncthreads();
     const uint32_t pos = s_excl + s_warp[warp];
@@ -514,6 +632,295 @@ __global__ void __launch_bounds__(kThreads) unique_kernel(const uint32_t* keys, 
     __syncthreads();  // shared state is reused by the next tile
     if (next_base >= m) return;
     tile = next;
+  }
+}
+
+// ---- unique by bitmap ------------------------------------------------------------
+// Bit b of the bitmap stands for key min + b.  All three kernels return at once
+// on the radix path.
+__global__ void __launch_bounds__(kThreads) bitmap_clear_kernel(const uint32_t* range, uint4* bitmap) {
+  if (range[2] != kBitmapPath) return;
+  const size_t n4 = ((size_t)range[3] + 3) / 4;
+  for (size_t i = blockIdx.x * (size_t)kThreads + threadIdx.x; i < n4; i += (size_t)gridDim.x * kThreads)
+    bitmap[i] = make_uint4(0u, 0u, 0u, 0u);
+}
+
+// Histogram of the range buckets (top 8 bits of key - min) of the kept keys;
+// the last CTA to finish turns the counts into offsets (no CTA waits).
+__global__ void __launch_bounds__(kThreads) range_hist_kernel(const uint32_t* keys, const int* count,
+                                                              const uint32_t* range, uint32_t* hist, int* done,
+                                                              uint32_t* cursors) {
+  __shared__ uint32_t sh[kBuckets];
+  __shared__ bool s_last;
+  if (range[2] != kBitmapPath) return;
+  const uint32_t m = (uint32_t)*count, lo = ~range[0];
+  const int shift = (int)range[4];
+  sh[threadIdx.x] = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  for (uint32_t i0 = blockIdx.x * kThreads * 8u; i0 < m; i0 += gridDim.x * kThreads * 8u) {
+    uint32_t k[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const uint32_t i = i0 + r * kThreads + threadIdx.x;
+      k[r] = i < m ? __ldg(keys + i) : 0u;
+    }
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {  // one shared atomic per distinct bucket per warp: frequent keys share one
+      const bool ok = i0 + r * kThreads + threadIdx.x < m;
+      const uint32_t b = ok ? (k[r] - lo) >> shift : 0x100u + (uint32_t)lane;
+      const unsigned peers = __match_any_sync(0xffffffffu, b);
+      if (ok && lane == __ffs(peers) - 1) atomicAdd(&sh[b], (uint32_t)__popc(peers));
+    }
+  }
+  __syncthreads();
+  if (sh[threadIdx.x]) atomicAdd(hist + kRangeCounts + threadIdx.x, sh[threadIdx.x]);
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(done, 1) == (int)gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  const uint32_t c = *(volatile uint32_t*)(hist + kRangeCounts + threadIdx.x);
+  sh[threadIdx.x] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t run = 0;
+    for (int d = 0; d < kBuckets; ++d) { const uint32_t v = sh[d]; sh[d] = run; run += v; }
+  }
+  __syncthreads();
+  hist[kRangeOffsets + threadIdx.x] = sh[threadIdx.x];
+  cursors[threadIdx.x * kCursorStride] = sh[threadIdx.x];
+}
+
+// Range partition of the bitmap path.  Unstable (the bitmap does not care
+// about order): tiles of 4096 keys, grid-strided; a key's slot in its range
+// bucket comes from a shared per-tile count (one atomic per distinct bucket
+// per warp), the tile claims one range per bucket from the bucket's cursor,
+// and the keys are staged in shared memory in bucket order so each bucket's
+// run goes out contiguously while the next tile's keys load.  No CTA waits on
+// another.
+__global__ void __launch_bounds__(kThreads, 4) range_partition_kernel(const uint32_t* in, uint32_t* out,
+                                                                   const int* count, const uint32_t* range,
+                                                                   uint32_t* cursors) {
+  __shared__ uint32_t s_cnt[kBuckets];    // per-tile count, then the tile-local start of each bucket
+  __shared__ uint32_t s_base[kBuckets];   // global start of each bucket's run
+  __shared__ uint32_t s_keys[kTile];
+  if (range[2] != kBitmapPath) return;
+  const uint32_t m = (uint32_t)*count, lo = ~range[0];
+  const int shift = (int)range[4];
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1;
+  const uint32_t stride = gridDim.x * (uint32_t)kTile;
+  uint32_t k[kItems];
+#pragma unroll
+  for (int r = 0; r < kItems; ++r) {
+    const uint32_t i = blockIdx.x * (uint32_t)kTile + r * kThreads + threadIdx.x;
+    k[r] = i < m ? __ldg(in + i) : 0u;
+  }
+  for (uint32_t base = blockIdx.x * (uint32_t)kTile; base < m; base += stride) {
+    const uint32_t valid = min((uint32_t)kTile, m - base);
+    s_cnt[threadIdx.x] = 0;
+    __syncthreads();
+    uint32_t slot[kItems / 2];  // two 16-bit slots (< 4096) per word
+#pragma unroll
+    for (int r = 0; r < kItems; ++r) {
+      const bool ok = r * kThreads + threadIdx.x < valid;
+      const uint32_t b = ok ? (k[r] - lo) >> shift : 0x100u + (uint32_t)lane;
+      const unsigned peers = __match_any_sync(0xffffffffu, b);
+      const int leader = __ffs(peers) - 1;
+      uint32_t first = 0;
+      if (ok && lane == leader) first = atomicAdd(&s_cnt[b], (uint32_t)__popc(peers));
+      first = __shfl_sync(0xffffffffu, first, leader);
+      const uint32_t sl = first + __popc(peers & lt);
+      slot[r / 2] = (r & 1) ? slot[r / 2] | (sl << 16) : sl;
+    }
+    __syncthreads();
+    {
+      const uint32_t c = s_cnt[threadIdx.x];
+      if (c) s_base[threadIdx.x] = atomicAdd(cursors + threadIdx.x * kCursorStride, c);
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {  // tile-local bucket starts: exclusive scan of 256 counts by one warp
+      uint32_t v[8], sum = 0;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) { v[q] = s_cnt[lane * 8 + q]; sum += v[q]; }
+      uint32_t incl = sum;
+      for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += t;
+      }
+      uint32_t run = incl - sum;
+      __syncwarp();
+#pragma unroll
+      for (int q = 0; q < 8; ++q) { s_cnt[lane * 8 + q] = run; run += v[q]; }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kItems; ++r)
+      if (r * kThreads + threadIdx.x < valid)
+        s_keys[s_cnt[(k[r] - lo) >> shift] + ((r & 1) ? slot[r / 2] >> 16 : slot[r / 2] & 0xffffu)] = k[r];
+    // the next tile's keys are in flight during the write-out
+#pragma unroll
+    for (int r = 0; r < kItems; ++r) {
+      const uint32_t i = base + stride + r * kThreads + threadIdx.x;
+      k[r] = i < m ? __ldg(in + i) : 0u;
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < valid; i += kThreads) {
+      const uint32_t key = s_keys[i];
+      const uint32_t b = (key - lo) >> shift;
+      out[s_base[b] + i - s_cnt[b]] = key;
+    }
+    __syncthreads();  // shared state is reused by the next tile
+  }
+}
+
+// One range bucket's bitmap slice (at most 2^18 bits) built in shared memory
+// from its partitioned keys (a shared atomicOr only for bits not yet set),
+// then OR-ed into the global bitmap word by word
+// (only words with bits set; a word shared with a neighbouring bucket is
+// combined by the atomic).  Work items are chunks of kChunk keys of one
+// bucket, claimed from a counter, so a bucket holding most keys (feedback is
+// Zipf-like) is spread over many CTAs.
+constexpr int kChunk = 16384;
+constexpr int kSliceWords = (1 << (kMaxSpanLog2 - 8)) / 32 + 1;
+__global__ void __launch_bounds__(kThreads) bucket_bitmap_kernel(const uint32_t* keys, const uint32_t* range,
+                                                                 const uint32_t* hist, uint32_t* bitmap,
+                                                                 int* item_counter) {
+  __shared__ uint32_t s_bits[kSliceWords];
+  __shared__ uint32_t s_first[kBuckets + 1];  // first item of each bucket; [256] = all items
+  __shared__ int s_item;
+  if (range[2] != kBitmapPath) return;
+  const uint32_t lo = ~range[0];
+  const int shift = (int)range[4];
+  const int lane = threadIdx.x & 31;
+  {  // items per bucket, scanned by one warp
+    const uint32_t c = hist[kRangeCounts + threadIdx.x];
+    s_first[threadIdx.x] = (c + kChunk - 1) / kChunk;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      uint32_t v[8], sum = 0;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) { v[k] = s_first[lane * 8 + k]; sum += v[k]; }
+      uint32_t incl = sum;
+      for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += t;
+      }
+      uint32_t run = incl - sum;
+      __syncwarp();
+#pragma unroll
+      for (int k = 0; k < 8; ++k) { s_first[lane * 8 + k] = run; run += v[k]; }
+      if (lane == 31) s_first[kBuckets] = run;
+    }
+    __syncthreads();
+  }
+  const uint32_t items = s_first[kBuckets];
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(item_counter, 1);
+    __syncthreads();
+    const uint32_t item = (uint32_t)s_item;
+    if (item >= items) return;
+    int b = 0;  // the bucket: last with s_first[b] <= item
+    for (int step = kBuckets / 2; step > 0; step >>= 1)
+      if (s_first[b + step] <= item) b += step;
+    const uint32_t count = hist[kRangeCounts + b];
+    const uint32_t first = hist[kRangeOffsets + b] + (item - s_first[b]) * kChunk;
+    const uint32_t end = hist[kRangeOffsets + b] + min(count, (item - s_first[b] + 1) * kChunk);
+    const uint32_t bit0 = (uint32_t)b << shift;  // the bucket's first bit
+    const uint32_t w0 = bit0 >> 5;
+    const int words = (int)(((bit0 + (1u << shift) - 1) >> 5) - w0 + 1);
+    for (int i = threadIdx.x; i < words; i += kThreads) s_bits[i] = 0;
+    __syncthreads();
+    for (uint32_t r0 = first; r0 < end; r0 += kThreads * 8) {  // the same rounds for every thread
+      uint32_t k[8];
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        const uint32_t i = r0 + r * kThreads + threadIdx.x;
+        k[r] = i < end ? __ldg(keys + i) : 0u;
+      }
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        if (r0 + r * kThreads + threadIdx.x >= end) continue;
+        const uint32_t bit = k[r] - lo;
+        const uint32_t word = (bit >> 5) - w0, mask = 1u << (bit & 31);
+        // a bit already set costs a (broadcast) load, not an atomic: frequent
+        // keys stop contending once set; two lanes racing both OR the same bit
+        if ((s_bits[word] & mask) == 0) atomicOr(s_bits + word, mask);
+      }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < words; i += kThreads)
+      if (s_bits[i]) atomicOr(bitmap + w0 + i, s_bits[i]);
+    __syncthreads();  // s_bits / s_item are reused by the next item
+  }
+}
+
+// The set bits in order, as signed words: tiles of 1024 bitmap words (4 per
+// thread, one 16-byte load), a CTA scan of the per-thread bit counts and a
+// look-back for the tile's output position.  Persistent like unique_kernel.
+// The last tile writes the count and the NO_HIT sentinel when any word was
+// NO_HIT.
+constexpr int kBitmapTile = kThreads * 4;
+__global__ void __launch_bounds__(kThreads) bitmap_unique_kernel(const uint32_t* bitmap, const int* count,
+                                                                 int n_total, const uint32_t* range, int32_t* out,
+                                                                 unsigned long long* status, int* tile_counter,
+                                                                 int* result) {
+  __shared__ int s_tile;
+  __shared__ uint32_t s_warp[kWarps + 1];
+  __shared__ uint32_t s_excl;
+  if (range[2] != kBitmapPath) return;
+  const uint32_t n_words = range[3], lo = ~range[0];
+  const int m = *count;
+  const uint32_t tag = g_epoch * 8u + 5u;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1);
+    __syncthreads();
+    const int tile = s_tile;
+    const size_t base = (size_t)tile * kBitmapTile;
+    if (base >= n_words) return;
+    const size_t first = base + (size_t)threadIdx.x * 4;
+    uint32_t w[4];
+    if (first + 4 <= n_words) {
+      const uint4 v = __ldg(reinterpret_cast<const uint4*>(bitmap + first));
+      w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w;
+    } else {
+#pragma unroll
+      for (int r = 0; r < 4; ++r) w[r] = first + r < n_words ? __ldg(bitmap + first + r) : 0u;
+    }
+    const uint32_t cnt = __popc(w[0]) + __popc(w[1]) + __popc(w[2]) + __popc(w[3]);
+    uint32_t incl = cnt;
+    for (int off = 1; off < 32; off <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, off);
+      if (lane >= off) incl += t;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+      const uint32_t excl = tile_prefix(s_warp, status, tile, tag);
+      if (lane == 0 && base + kBitmapTile >= n_words) {  // last tile
+        int u = min((int)(excl + s_warp[kWarps]), m);
+        if (m < n_total) out[u++] = kNoHit;
+        *result = u;
+      }
+      if (lane == 0) s_excl = excl;
+    }
+    __syncthreads();
+    uint32_t pos = s_excl + s_warp[warp] + incl - cnt;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      uint32_t v = w[r];
+      const uint32_t key0 = lo + (uint32_t)(first + r) * 32u;
+      while (v) {
+        const int b = __ffs(v) - 1;
+        v &= v - 1;
+        if (pos < (uint32_t)m) out[pos] = (int32_t)((key0 + (uint32_t)b) ^ 0x80000000u);
+        ++pos;
+      }
+    }
+    __syncthreads();  // s_tile / s_warp / s_excl are reused by the next tile
   }
 }
 
@@ -583,37 +990,36 @@ int grid_for(int n) {
   return tiles > 0 ? tiles : 1;
 }
 
-// Resident CTAs of a persistent kernel, at most the tiles of n keys.
-template <typename Kernel>
-int persistent_grid(Kernel k, int n) {
+// Resident CTAs of persistent kernel K, at most the tiles of n keys.
+template <auto K>
+int persistent_grid(int n) {
   static int resident = 0;
   if (!resident) {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, K, kThreads, 0);
     resident = sms * (per_sm > 0 ? per_sm : 1);
   }
   return std::min(resident, grid_for(n));
 }
 
+// The four digit passes.  With `range` (feedback unique) they return at once
+// when the bitmap path was chosen.
 cudaError_t run_passes(SortScratchLayout& l, int n, uint32_t*& cur, uint32_t*& other, int32_t* final_out,
-                       cudaStream_t s) {
+                       const uint32_t* range, cudaStream_t s) {
   cudaError_t e;
-  hist_offsets_kernel<<<1, kBuckets, 0, s>>>(l.hist);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  const int grid = persistent_grid(digit_kernel, n);
+  const int grid = persistent_grid<digit_kernel>(n);
   for (int p = 0; p < kPasses; ++p) {
     const bool last = p == kPasses - 1;
     digit_kernel<<<grid, kThreads, 0, s>>>(cur, other, l.count, 8 * p, l.hist + p * kBuckets, l.status,
-                                           l.tile_counter + p, p, last, last ? final_out : nullptr);
+                                                  l.tile_counter + p, p, last, last ? final_out : nullptr, range);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     std::swap(cur, other);
   }
   return cudaSuccess;
 }
 
-// One wave of resident compaction CTAs, at most the tiles of n words.
 int compact_grid(int n) {
   static int resident = 0;
   if (!resident) {
@@ -665,16 +1071,33 @@ cudaError_t feedback_unique_device(const int32_t* words, int n, int nib, int32_t
   SortScratchLayout l = layout(scratch, n);
   if (scratch_bytes < l.bytes) return cudaErrorInvalidValue;
   cudaError_t e;
-  if ((e = cudaMemsetAsync(l.hist, 0, kPasses * kBuckets * 4, s)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(l.hist, 0, kHistRows * kBuckets * 4, s)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(l.tile_counter, 0, 16 * 4, s)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(l.count, 0, 4 * 4, s)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(l.range, 0, 8 * 4, s)) != cudaSuccess) return e;
   const int grid = compact_grid(n);
-  if ((e = launch_compact<true>(grid, words, n, nib, l.keys_a, l.count, l.hist, s)) != cudaSuccess) return e;
+  if ((e = launch_compact<true>(grid, words, n, nib, l.keys_a, l.count, l.hist, l.range, s)) != cudaSuccess)
+    return e;
+  hist_offsets_kernel<<<1, kBuckets, 0, s>>>(l.hist, l.count, l.range, l.bitmap_bits);
+  // bitmap path (each kernel returns at once on the radix path): range
+  // partition keys_a -> keys_b, bitmap in keys_a, its set bits in order
+  const int grid_n = std::min(grid, std::max(1, (int)(((size_t)n + 4095) / 4096)));
+  range_hist_kernel<<<grid_n, kThreads, 0, s>>>(l.keys_a, l.count, l.range, l.hist, l.tile_counter + kCtrRangeDone,
+                                                l.cursors);
+  range_partition_kernel<<<grid_n, kThreads, 0, s>>>(l.keys_a, l.keys_b, l.count, l.range, l.cursors);
+  bitmap_clear_kernel<<<grid_n, kThreads, 0, s>>>(l.range, reinterpret_cast<uint4*>(l.keys_a));
+  bucket_bitmap_kernel<<<persistent_grid<bucket_bitmap_kernel>(n), kThreads, 0, s>>>(
+      l.keys_b, l.range, l.hist, l.keys_a, l.tile_counter + kCtrBuckets);
+  bitmap_unique_kernel<<<persistent_grid<bitmap_unique_kernel>(n), kThreads, 0, s>>>(
+      l.keys_a, l.count, n, l.range, unique_out, l.status, l.tile_counter + kCtrBitmapUnique, counts_dev);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  // radix path (each kernel returns at once on the bitmap path)
   uint32_t* cur = l.keys_a;
   uint32_t* other = l.keys_b;
-  if ((e = run_passes(l, n, cur, other, nullptr, s)) != cudaSuccess) return e;
-  unique_kernel<<<persistent_grid(unique_kernel, n), kThreads, 0, s>>>(cur, l.count, n, unique_out, l.status,
-                                                                      l.tile_counter + kPasses, counts_dev);
+  if ((e = run_passes(l, n, cur, other, nullptr, l.range, s)) != cudaSuccess) return e;
+  unique_kernel<<<persistent_grid<unique_kernel>(n), kThreads, 0, s>>>(cur, l.count, n, unique_out, l.status,
+                                                                      l.tile_counter + kCtrUnique, counts_dev,
+                                                                      l.range);
   return cudaGetLastError();
 }
 
@@ -688,10 +1111,12 @@ cudaError_t sort_i32_device(int32_t* data, int n, void* scratch, size_t scratch_
   if ((e = cudaMemsetAsync(l.count, 0, 4 * 4, s)) != cudaSuccess) return e;
   if ((e = launch_fill_i32(l.count, n, 1, s)) != cudaSuccess) return e;  // [0] keys; [2] the compaction's claims
   const int grid = compact_grid(n);
-  if ((e = launch_compact<false>(grid, data, n, 0, l.keys_a, l.count + 2, l.hist, s)) != cudaSuccess) return e;
+  if ((e = launch_compact<false>(grid, data, n, 0, l.keys_a, l.count + 2, l.hist, nullptr, s)) != cudaSuccess)
+    return e;
+  hist_offsets_kernel<<<1, kBuckets, 0, s>>>(l.hist, l.count, nullptr, 0);
   uint32_t* cur = l.keys_a;
   uint32_t* other = l.keys_b;
-  return run_passes(l, n, cur, other, data, s);
+  return run_passes(l, n, cur, other, data, nullptr, s);
 }
 
 cudaError_t scan_i32_device(int32_t* data, int n, void* scratch, size_t scratch_bytes, cudaStream_t s) {

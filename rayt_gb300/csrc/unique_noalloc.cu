@@ -37,13 +37,14 @@ constexpr size_t kCountsBytes = 256;
 // Sort/unique scratch for kMaxWords words plus 256 bytes for the result count.
 // feedback_scratch_bytes() is a host function, so the size is computed from the
 // same layout rules here: two key arrays of (n + 4) words rounded to 256 bytes,
-// 4 x 256 histogram words, one 8-byte look-back word per 256 buckets per
-// 4096-key tile (+1 tile), 16 tile counters and 4 counts, each rounded to 256
-// bytes.
+// 6 x 256 histogram words, one 8-byte look-back word per 256 buckets per
+// 4096-key tile (+1 tile), 16 tile counters, 4 counts, 8 key-range words and
+// 256 partition cursors 128 bytes apart, each rounded to 256 bytes.
 constexpr size_t Up256(size_t v) { return (v + 255) & ~(size_t)255; }
 constexpr size_t kTiles = ((size_t)kMaxWords + 4095) / 4096 + 1;
-constexpr size_t kScratchBytes = 2 * Up256((size_t)kMaxWords * 4 + 16) + Up256(4 * 256 * 4) +
-                                 Up256(kTiles * 256 * 8) + Up256(16 * 4) + Up256(4 * 4);
+constexpr size_t kScratchBytes = 2 * Up256((size_t)kMaxWords * 4 + 16) + Up256(6 * 256 * 4) +
+                                 Up256(kTiles * 256 * 8) + Up256(16 * 4) + Up256(4 * 4) + Up256(8 * 4) +
+                                 Up256(256 * 32 * 4);
 
 static __device__ __align__(256) uint8_t g_noalloc_scratch[kScratchBytes + kCountsBytes];
 

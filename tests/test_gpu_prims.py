@@ -99,6 +99,69 @@ def test_feedback_unique_large_properties(built, n):
     assert np.all(np.diff(u.astype(np.int64)) > 0) and u[-1] == NO_HIT
 
 
+def _np_unique(words, nib):
+    conv = words.astype(np.int64)
+    hit = (conv > 0) & (conv != NO_HIT)
+    if nib > 0:
+        conv[hit] = ((((conv[hit] >> 1) - 1) // nib + 1) << 1) | (conv[hit] & 1)
+    return np.unique(conv).astype(np.int32)
+
+
+def _bitmap_path(words, nib):
+    """True when feedback unique takes the bitmap path: the kept keys span at
+    most the bitmap's capacity, 8 bits per byte of one (n + 4)-word key buffer
+    in whole 16-byte units."""
+    u = _np_unique(words, nib).astype(np.int64)
+    u = u[u != NO_HIT]
+    cap = ((words.size * 4 + 16) // 16) * 16 * 8
+    return u.size > 0 and int(u.max() - u.min() + 1) <= cap
+
+
+@pytest.mark.parametrize("case", ["narrow", "narrow_no_nohit", "one_key", "top_end", "bottom_end", "wide_small_n",
+                                  "cap_exact", "cap_plus_one", "zipf_heavy"])
+def test_feedback_unique_bitmap_and_radix_paths(built, case):
+    """Feedback unique takes the bitmap path when the kept keys span at most 32
+    values per input word and the radix passes otherwise; both give the sorted
+    unique set."""
+    rng = np.random.default_rng(sum(map(ord, case)))
+    n, nib = 200_000, 0
+    if case == "narrow":
+        words = rng.integers(-5000, 5000, n).astype(np.int32)
+        words[rng.random(n) < 0.7] = NO_HIT
+        path = True
+    elif case == "narrow_no_nohit":
+        words, nib, path = feedback_words(n, 3, no_hit=False, id_bits=12), 64, True
+    elif case == "one_key":
+        words = np.full(n, -77, np.int32)
+        words[::3] = NO_HIT
+        path = True
+    elif case == "top_end":
+        words = (2**31 - 2 - rng.integers(0, 3000, n)).astype(np.int32)
+        path = True
+    elif case == "bottom_end":
+        words = (-2**31 + rng.integers(0, 3000, n)).astype(np.int32)
+        path = True
+    elif case == "wide_small_n":
+        n = 5000
+        words = rng.integers(-2**31, 2**31 - 1, n, dtype=np.int64).astype(np.int32)
+        path = False
+    elif case in ("cap_exact", "cap_plus_one"):
+        n = 1000
+        cap = ((n * 4 + 16) // 16) * 16 * 8
+        words = np.full(n, NO_HIT, np.int32)
+        words[10] = -100000
+        words[500] = -100000 + cap - 1 + (case == "cap_plus_one")
+        words[700] = -100000 + 5
+        path = case == "cap_exact"
+    else:  # zipf_heavy: a few keys repeated very often, as feedback is
+        n = 1 << 22
+        ids = np.minimum(rng.zipf(1.3, n), 1 << 20)
+        words = np.where(rng.random(n) < 0.5, -ids, (ids << 1) | 1).astype(np.int32)
+        nib, path = 1, True
+    assert _bitmap_path(words, nib) == path
+    np.testing.assert_array_equal(_unique(words, nib), _np_unique(words, nib))
+
+
 @pytest.mark.parametrize("offset", [1, 2, 3])
 def test_unaligned_inputs(built, offset):
     """Input arrays that start off a 16-byte boundary take the scalar-load
