@@ -352,6 +352,7 @@ def bench_frames(args, rank, world, local):
     clocks.start()
     ms_dev, wall = 0.0, 0.0
     passes, launches, h2d, d2h, uploaded, trace_ms = 0, 0, 0, 0, 0, 0.0
+    part_ms = {k: 0.0 for k in ("gpu_ms_feedback", "gpu_ms_upload", "host_ms_wait", "host_ms_decode", "host_ms_load")}
     lat = []
     for i in range(args.warmup, args.warmup + steps):
         with torch.cuda.stream(stream):
@@ -376,6 +377,8 @@ def bench_frames(args, rank, world, local):
         d2h += st["bytes_d2h"] + w * h * 4
         uploaded += st["uploaded_blocks"]
         trace_ms += st["gpu_ms_trace"]
+        for k in part_ms:
+            part_ms[k] += st[k]
     torch.cuda.synchronize()
     barrier(world)
     clk = clocks.stop()
@@ -416,7 +419,8 @@ def bench_frames(args, rank, world, local):
         "frame_latency_ms": {"p50": round(float(np.percentile(lat_sorted, 50)), 4),
                              "p99": round(float(np.percentile(lat_sorted, 99)), 4)},
         "frames": {"passes_per_frame": round(passes / steps, 3), "uploaded_blocks_per_frame": round(uploaded / steps, 2),
-                   "trace_ms_per_frame": round(trace_ms / steps, 4)},
+                   "trace_ms_per_frame": round(trace_ms / steps, 4),
+                   **{k.replace("_ms_", "_") + "_ms_per_frame": round(v / steps, 4) for k, v in part_ms.items()}},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
                      "kernel": "trace_kernel<first pass>", "launch_ms": round(pass_ms, 4),

@@ -217,6 +217,7 @@ int Cache::Init(Tree* tree, int max_blocks) {
   slots_.resize((size_t)max_blocks_);
   block_slot_.assign(tree->info.blocks_count, -1);
   parent_slot_.assign(tree->info.blocks_count, -1);
+  validated_.assign(tree->info.blocks_count, 0);
   touched_.assign((size_t)max_blocks_, 0);
   const int ids = max_blocks_ + kMarkers + 1;
   prev_.assign(ids, -1);
@@ -437,6 +438,11 @@ int Cache::ReadOne(int pos, int block) {
     }
   }
   const uint32_t* links = reinterpret_cast<const uint32_t*>(area + 80);
+  if (validated_[block]) {  // links checked on an earlier load: only the fault children
+    for (int n = 0; n < nib_; ++n)
+      if ((links[n] & 255u) && ((links[n] >> 8) & 1u)) m.faults.push_back(links[n] >> 11);
+    return RAYT_OK;
+  }
   for (int n = 0; n < nib_; ++n) {
     const uint32_t l = links[n], mask = l & 255u, ptr = l >> 11;
     if (!mask) continue;
@@ -449,6 +455,7 @@ int Cache::ReadOne(int pos, int block) {
     if (ptr >= blocks) return bad("fault link points past the last block");
     m.faults.push_back(ptr);
   }
+  validated_[block] = 1;  // one byte per block: threads reading other blocks touch other bytes
   return RAYT_OK;
 }
 

@@ -75,6 +75,7 @@ class Cache {
   std::vector<Slot> slots_;
   std::vector<int32_t> block_slot_;    // tree block -> cache slot, -1 absent
   std::vector<int32_t> parent_slot_;   // tree block -> slot of its parent, -1 absent
+  std::vector<uint8_t> validated_;     // tree block -> its links passed the check once (the file is read-only)
   std::vector<int> pending_;
   bool in_session_ = false, in_transaction_ = false;
 
