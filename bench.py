@@ -882,6 +882,34 @@ def c2_path(words, nib):
     return int(w.size), span <= cap and span <= (1 << 26), span
 
 
+def time_primitives(R, n, steps):
+    """GPUSort and GPUScan (in place) on n uniform random int32, each call on a
+    fresh copy of the input; CUDA events around the call only."""
+    import torch
+    g = torch.Generator(device="cuda")
+    g.manual_seed(13)
+    src = torch.randint(-2**31, 2**31 - 1, (n,), dtype=torch.int32, device="cuda", generator=g)
+    x = torch.empty_like(src)
+    out = {}
+    for name, fn in (("GPUSort", R.GPUSort), ("GPUScan", R.GPUScan)):
+        ms = 0.0
+        reps = max(3, min(steps, 10))
+        for k in range(reps + 2):
+            x.copy_(src)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn(x, n)
+            e1.record()
+            e1.synchronize()
+            if k >= 2:
+                ms += e0.elapsed_time(e1)
+        ms /= reps
+        out[name] = {"n": n, "ms": round(ms, 4), "gkeys_s": round(n / ms / 1e6, 2), "calls": reps,
+                     "input": "uniform random int32, in place"}
+    del src, x
+    return out
+
+
 def bench_c2(args, rank, world, local):
     import torch
 
@@ -927,6 +955,7 @@ def bench_c2(args, rank, world, local):
     e1.record()
     torch.cuda.synchronize()
     t_dev = max_over_ranks(e0.elapsed_time(e1) / 1e3, world)
+    prims = time_primitives(R, n, steps)
     # end to end: words from pinned host memory, unique array back to host
     t = time.perf_counter()
     for _ in range(steps):
@@ -969,7 +998,7 @@ def bench_c2(args, rank, world, local):
                          "peak_source": kind,
                          "kernel": ("compaction + range partition + bucket bitmaps + bitmap unique (one call)" if bitmap
                                     else "compaction + 4 digit passes + unique (one call)")},
-            "cpu_baseline": cpu, "gpu_launches": steps * 12, "clocks": clk}
+            "cpu_baseline": cpu, "gpu_launches": steps * 12, "clocks": clk, "primitives": prims}
 
 
 def main():

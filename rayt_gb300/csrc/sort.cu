@@ -925,10 +925,13 @@ __global__ void __launch_bounds__(kThreads) bitmap_unique_kernel(const uint32_t*
 }
 
 // ---- inclusive scan (wrapping int32) ---------------------------------------------
+// Tiles of 4096 values claimed in order; a tile's prefix comes from a warp-wide
+// look-back over a status table cleared per call (tag 0: a cleared word is
+// unpublished).  Sums wrap like the reference's int arithmetic.
 __global__ void __launch_bounds__(kThreads) scan_kernel(int32_t* data, int n, unsigned long long* status,
                                                         int* tile_counter) {
   __shared__ int s_tile;
-  __shared__ uint32_t s_warp[kWarps];
+  __shared__ uint32_t s_warp[kWarps + 1];
   __shared__ uint32_t s_excl;
   if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1);
   __syncthreads();
@@ -937,12 +940,19 @@ __global__ void __launch_bounds__(kThreads) scan_kernel(int32_t* data, int n, un
   if (base >= n) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   uint32_t v[kItems], sum = 0;
+  const int first = base + threadIdx.x * kItems;
+  if (first + kItems <= n && ((reinterpret_cast<uintptr_t>(data + first) & 15) == 0)) {
 #pragma unroll
-  for (int r = 0; r < kItems; ++r) {
-    const int i = base + threadIdx.x * kItems + r;
-    v[r] = i < n ? (uint32_t)data[i] : 0u;
-    sum += v[r];
+    for (int r = 0; r < kItems / 4; ++r) {
+      const int4 q = reinterpret_cast<const int4*>(data + first)[r];
+      v[4 * r] = (uint32_t)q.x; v[4 * r + 1] = (uint32_t)q.y; v[4 * r + 2] = (uint32_t)q.z; v[4 * r + 3] = (uint32_t)q.w;
+    }
+  } else {
+#pragma unroll
+    for (int r = 0; r < kItems; ++r) v[r] = first + r < n ? (uint32_t)data[first + r] : 0u;
   }
+#pragma unroll
+  for (int r = 0; r < kItems; ++r) sum += v[r];
   uint32_t incl = sum;
   for (int off = 1; off < 32; off <<= 1) {
     const uint32_t t = __shfl_up_sync(0xffffffffu, incl, off);
@@ -950,38 +960,26 @@ __global__ void __launch_bounds__(kThreads) scan_kernel(int32_t* data, int n, un
   }
   if (lane == 31) s_warp[warp] = incl;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    uint32_t run = 0;
-    for (int w = 0; w < kWarps; ++w) { const uint32_t t = s_warp[w]; s_warp[w] = run; run += t; }
-    const unsigned long long agg = 1ull << 32, pre = 2ull << 32;
-    unsigned long long* st = status + tile;
-    if (tile == 0) {
-      *(volatile unsigned long long*)st = pre | run;
-      s_excl = 0;
-    } else {
-      *(volatile unsigned long long*)st = agg | run;
-      uint32_t excl = 0;
-      for (int j = tile - 1; j >= 0; --j) {
-        unsigned long long s;
-        long long spins = 0;
-        const unsigned long long start = global_ns();
-        while (((s = ld_volatile64(status + j)) >> 32) == 0) {
-          if (wait_over(spins, start)) { atomicExch(&g_error_flag, 1); break; }
-        }
-        excl += (uint32_t)s;
-        if ((s >> 32) == 2 || (s >> 32) == 0) break;
-      }
-      *(volatile unsigned long long*)st = pre | (uint32_t)(excl + run);
-      s_excl = excl;
-    }
+  if (warp == 0) {
+    const uint32_t excl = tile_prefix(s_warp, status, tile, 0u);
+    if (lane == 0) s_excl = excl;
   }
   __syncthreads();
   uint32_t run = s_excl + s_warp[warp] + incl - sum;
 #pragma unroll
   for (int r = 0; r < kItems; ++r) {
-    const int i = base + threadIdx.x * kItems + r;
     run += v[r];
-    if (i < n) data[i] = (int32_t)run;
+    v[r] = run;
+  }
+  if (first + kItems <= n && ((reinterpret_cast<uintptr_t>(data + first) & 15) == 0)) {
+#pragma unroll
+    for (int r = 0; r < kItems / 4; ++r)
+      reinterpret_cast<int4*>(data + first)[r] =
+          make_int4((int)v[4 * r], (int)v[4 * r + 1], (int)v[4 * r + 2], (int)v[4 * r + 3]);
+  } else {
+#pragma unroll
+    for (int r = 0; r < kItems; ++r)
+      if (first + r < n) data[first + r] = (int32_t)v[r];
   }
 }
 
