@@ -452,8 +452,11 @@ __global__ void __launch_bounds__(kThreads, 4) digit_kernel(const uint32_t* in, 
     const int valid = min(kTile, m - base);
     if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1);  // the next tile
 
-    // ranking; the keys are already in registers, so the rounds' __syncwarp
-    // (which orders memory) holds up no loads
+    // ranking (stable): per round, the lanes holding a digit take consecutive
+    // ranks after the warp's earlier keys of that digit.  The group's first
+    // lane adds the group to the warp's shared count with one atomic and
+    // shares the old count; the next round's atomic is issued after that
+    // shuffle has read this one's result, so rounds apply in order.
     uint32_t ranks[kItems / 2];  // two 16-bit ranks (< 512) per word
 #pragma unroll
     for (int r = 0; r < kItems; ++r) {
@@ -461,13 +464,13 @@ __global__ void __launch_bounds__(kThreads, 4) digit_kernel(const uint32_t* in, 
       const bool ok = li < valid;
       const uint32_t d = ok ? (keys[r] >> shift) & 255u : 0x100u + (uint32_t)lane;  // invalid keys match nobody
       const unsigned peers = __match_any_sync(0xffffffffu, d);
-      const uint32_t before = ok ? s_warp[warp][d] : 0u;
+      const int leader = __ffs(peers) - 1;
+      uint32_t before = 0;
+      if (ok && lane == leader) before = atomicAdd(&s_warp[warp][d], (uint32_t)__popc(peers));
+      before = __shfl_sync(0xffffffffu, before, leader);
       const uint32_t rank = before + __popc(peers & ((1u << lane) - 1));
       ranks[r / 2] = (r & 1) ? ranks[r / 2] | (rank << 16) : rank;
       if (ok) s_in[li] = keys[r];  // parked in shared memory until the staging step
-      __syncwarp();
-      if (ok && lane == __ffs(peers) - 1) s_warp[warp][d] = before + __popc(peers);
-      __syncwarp();
     }
     __syncthreads();
     const int next = s_tile;
