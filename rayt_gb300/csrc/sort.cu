@@ -410,8 +410,11 @@ __global__ void hist_offsets_kernel(uint32_t* hist, const int* count, uint32_t* 
 }
 
 // The lanes of the warp holding the same 8-bit digit d (a lane whose key is
-// not valid is alone): one ballot per digit bit, measured 8-11% faster per
-// sort than __match_any_sync on the digit.
+// not valid is alone): one ballot per digit bit.  On uniform digits this was
+// 8-11% faster per sort than __match_any_sync; on the Zipf-skewed range
+// buckets of feedback, where few distinct values share a warp,
+// __match_any_sync is faster (2.5x in the range histogram), so those kernels
+// keep it.
 __device__ __forceinline__ unsigned digit_peers(uint32_t d, bool ok) {
   unsigned peers = __ballot_sync(0xffffffffu, ok);
   peers = ok ? peers : (1u << (threadIdx.x & 31));
