@@ -109,16 +109,16 @@ def _np_unique(words, nib):
 
 def _bitmap_path(words, nib):
     """True when feedback unique takes the bitmap path: the kept keys span at
-    most the bitmap's capacity, 8 bits per byte of one (n + 4)-word key buffer
-    in whole 16-byte units."""
+    most 2^26 values and at most the bitmap's capacity, 8 bits per byte of one
+    (n + 4)-word key buffer in whole 16-byte units."""
     u = _np_unique(words, nib).astype(np.int64)
     u = u[u != NO_HIT]
     cap = ((words.size * 4 + 16) // 16) * 16 * 8
-    return u.size > 0 and int(u.max() - u.min() + 1) <= cap
+    return u.size > 0 and int(u.max() - u.min() + 1) <= min(cap, 1 << 26)
 
 
 @pytest.mark.parametrize("case", ["narrow", "narrow_no_nohit", "one_key", "top_end", "bottom_end", "wide_small_n",
-                                  "cap_exact", "cap_plus_one", "zipf_heavy"])
+                                  "cap_exact", "cap_plus_one", "zipf_heavy", "span_2_26", "span_over_2_26"])
 def test_feedback_unique_bitmap_and_radix_paths(built, case):
     """Feedback unique takes the bitmap path when the kept keys span at most 32
     values per input word and the radix passes otherwise; both give the sorted
@@ -153,6 +153,11 @@ def test_feedback_unique_bitmap_and_radix_paths(built, case):
         words[500] = -100000 + cap - 1 + (case == "cap_plus_one")
         words[700] = -100000 + 5
         path = case == "cap_exact"
+    elif case in ("span_2_26", "span_over_2_26"):  # the widest bitmap (2^18-bit range slices), and one past it
+        n = (1 << 21) + 77
+        words = rng.integers(-(1 << 25), (1 << 25) - 1, n).astype(np.int32)
+        words[0], words[1] = -(1 << 25), (1 << 25) - 1 + (case == "span_over_2_26")
+        path = case == "span_2_26"
     else:  # zipf_heavy: a few keys repeated very often, as feedback is
         n = 1 << 22
         ids = np.minimum(rng.zipf(1.3, n), 1 << 20)
