@@ -44,8 +44,9 @@ constexpr int kPasses = 4;
 // histogram rows: the four digits, then the range buckets' counts and offsets
 constexpr int kHistRows = kPasses + 2;
 constexpr int kRangeCounts = kPasses * kBuckets, kRangeOffsets = (kPasses + 1) * kBuckets;
-// the range partition's per-bucket cursors, one per 128-byte line: every tile
-// claims from most of them, and cursors sharing a line would share one L2 slice
+// the range partition's per-bucket cursors, one per 128-byte line, so that
+// claims on different buckets (every tile claims from most of them) never
+// contend for one line
 constexpr int kCursorStride = 32;
 // tile counters: digit passes 0-3, unique, bitmap unique, range histogram done
 // count, bucket items
