@@ -118,7 +118,8 @@ def _bitmap_path(words, nib):
 
 
 @pytest.mark.parametrize("case", ["narrow", "narrow_no_nohit", "one_key", "top_end", "bottom_end", "wide_small_n",
-                                  "cap_exact", "cap_plus_one", "zipf_heavy", "span_2_26", "span_over_2_26"])
+                                  "cap_exact", "cap_plus_one", "zipf_heavy", "span_2_26", "span_over_2_26",
+                                  "wide_large_n"])
 def test_feedback_unique_bitmap_and_radix_paths(built, case):
     """Feedback unique takes the bitmap path when the kept keys span at most 32
     values per input word and the radix passes otherwise; both give the sorted
@@ -153,6 +154,12 @@ def test_feedback_unique_bitmap_and_radix_paths(built, case):
         words[500] = -100000 + cap - 1 + (case == "cap_plus_one")
         words[700] = -100000 + 5
         path = case == "cap_exact"
+    elif case == "wide_large_n":  # the radix passes at scale: keys over the whole int32 range
+        n = (1 << 22) + 5
+        words = rng.integers(-2**31, 2**31 - 1, n, dtype=np.int64).astype(np.int32)
+        words[rng.random(n) < 0.5] = NO_HIT
+        words[:1000] = words[1000:2000]  # some repeats
+        path = False
     elif case in ("span_2_26", "span_over_2_26"):  # the widest bitmap (2^18-bit range slices), and one past it
         n = (1 << 21) + 77
         words = rng.integers(-(1 << 25), (1 << 25) - 1, n).astype(np.int32)
