@@ -19,14 +19,15 @@
 //                    bitmap in shared memory (so frequent keys cost no global
 //                    atomics), bitmap_unique writes the set bits in order,
 //   radix path       (wider ranges, and GPUSort) four stable digit_kernel
-//                    passes (tiles of 4096 keys, warp match_any ranking,
+//                    passes (tiles of 4096 keys, warp ballot ranking,
 //                    per-digit decoupled look-back, scatter staged through
 //                    shared memory) and unique_kernel (run starts counted per
 //                    tile with a look-back prefix).
-// The kernels of the path not taken return at once.  The persistent kernels
-// claim tile ids in order from an atomic counter until the device-side count
-// runs out, so a tile only waits on tiles claimed by running CTAs.  Look-back
-// words are tagged with a per-call epoch and the pass, so the table is never
+// The kernels of the path not taken return at once.  Tiles are claimed in
+// order from an atomic counter, by one CTA per tile (GPUSort, the scan) or by
+// persistent CTAs until the device-side count runs out (feedback unique), so a
+// tile only waits on tiles claimed by running CTAs.  The sort's look-back words
+// are tagged with a per-call epoch and the pass, so its table is never
 // cleared.  Every wait is bounded and sets an error flag instead of hanging.
 #include <algorithm>
 
