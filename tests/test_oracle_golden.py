@@ -82,6 +82,32 @@ def test_oracle_feedback_unique_golden(built):
         np.testing.assert_array_equal(out, d[key + "_unique"], err_msg=key)
 
 
+@pytest.mark.parametrize("seed", range(6))
+def test_oracle_feedback_unique_properties(built, seed):
+    """The oracle's restatement of GetUnique (merge sort, flag, Hillis-Steele
+    scan, compress) on random words of every kind (NO_HIT, faults, hits with
+    and without the duplicate bit, the int32 extremes) equals NodeToBlock then
+    numpy's sorted unique; n includes sizes around the reference's work-group
+    size and powers of two."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(seed)
+    for n in [1, 2, 255, 256, 257, 1023, 4096, 5000]:
+        nib = int(rng.choice([0, 1, 7, 512, 4096]))
+        kind = rng.integers(0, 4, n)
+        words = np.where(kind == 0, 0x7FFFFFFF,
+                         np.where(kind == 1, -rng.integers(1, 1 << 20, n),
+                                  (rng.integers(1, 1 << 24, n) << 1) | rng.integers(0, 2, n))).astype(np.int64)
+        if n > 3:
+            words[:3] = [-2**31, 2**30 - 1, 0x7FFFFFFF]
+        words = words.astype(np.int32)
+        conv = words.astype(np.int64)
+        hit = (conv > 0) & (conv != 0x7FFFFFFF)
+        if nib > 0:
+            conv[hit] = ((((conv[hit] >> 1) - 1) // nib + 1) << 1) | (conv[hit] & 1)
+        np.testing.assert_array_equal(O.feedback_unique(words, nib), np.unique(conv).astype(np.int32),
+                                      err_msg="n=%d nib=%d" % (n, nib))
+
+
 def test_golden_inputs_regenerate(built):
     """The committed feedback inputs are what common.feedback_words produces."""
     from tests.golden.common import feedback_words
