@@ -46,6 +46,54 @@ int check_device_error(cudaStream_t s) {
   }
   return RAYT_OK;
 }
+
+// rayt_feedback_unique's device work (4 memsets and 12 kernels, most of them
+// short or returning at once) as one CUDA graph, replayed while the call's
+// arguments repeat (a frame loop calls with the same buffers every frame):
+// one graph launch instead of 16 stream operations.  The count and the
+// device error flag come back in one copy into pinned memory.
+struct UniqueGraph {
+  const int32_t* words = nullptr;
+  int n = 0, nib = 0;
+  int32_t* out = nullptr;
+  void* scratch = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t capture = nullptr;  // private stream the graph is captured on
+  int* host = nullptr;             // pinned: [0] unique count, [1] error flag
+};
+UniqueGraph g_unique[64];
+
+// Launches the device work of one call on s: the cached graph when the
+// arguments match, else a newly captured one; direct launches if capture
+// fails.  Then queues the read-back of the count and the error flag.
+int unique_launch(int dev, const int32_t* words, int n, int nib, int32_t* out, void* scratch, size_t bytes,
+                  int* counts, cudaStream_t s, int** host) {
+  UniqueGraph& g = g_unique[dev];
+  if (!g.host) RAYT_CUDA_TRY(cudaHostAlloc(&g.host, 2 * sizeof(int), cudaHostAllocDefault));
+  if (!g.capture) RAYT_CUDA_TRY(cudaStreamCreateWithFlags(&g.capture, cudaStreamNonBlocking));
+  const bool same = g.exec && g.words == words && g.n == n && g.nib == nib && g.out == out && g.scratch == scratch;
+  if (!same) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g.exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(g.capture, cudaStreamCaptureModeRelaxed) == cudaSuccess) {
+      const cudaError_t le = feedback_unique_device(words, n, nib, out, counts, scratch, bytes, g.capture);
+      const cudaError_t ce = cudaStreamEndCapture(g.capture, &graph);
+      if (le == cudaSuccess && ce == cudaSuccess && graph &&
+          cudaGraphInstantiate(&g.exec, graph, 0) != cudaSuccess)
+        g.exec = nullptr;
+      if (graph) cudaGraphDestroy(graph);
+    }
+    cudaGetLastError();  // a failed capture leaves its error behind; the launches below report their own
+    g.words = words, g.n = n, g.nib = nib, g.out = out, g.scratch = scratch;
+  }
+  if (g.exec) RAYT_CUDA_TRY(cudaGraphLaunch(g.exec, s));
+  else RAYT_CUDA_TRY(feedback_unique_device(words, n, nib, out, counts, scratch, bytes, s));
+  RAYT_CUDA_TRY(cudaMemcpyAsync(g.host, counts, sizeof(int), cudaMemcpyDeviceToHost, s));
+  RAYT_CUDA_TRY(cudaMemcpyAsync(g.host + 1, device_error_flag(), sizeof(int), cudaMemcpyDeviceToHost, s));
+  *host = g.host;
+  return RAYT_OK;
+}
 }  // namespace
 }  // namespace rayt
 
@@ -106,12 +154,18 @@ int rayt_feedback_unique(const int32_t* words, int n, int nib, int32_t* unique, 
   int rc = rayt::get_scratch(bytes, &scratch);
   if (rc != RAYT_OK) return rc;
   int* counts = reinterpret_cast<int*>(static_cast<uint8_t*>(scratch) + (bytes - 256));
-  RAYT_CUDA_TRY(rayt::feedback_unique_device(words, n, nib, unique, counts, scratch, bytes - 256, s));
-  int host = 0;
-  RAYT_CUDA_TRY(cudaMemcpyAsync(&host, counts, 4, cudaMemcpyDeviceToHost, s));
-  rc = rayt::check_device_error(s);
+  int dev = 0;
+  RAYT_CUDA_TRY(cudaGetDevice(&dev));
+  int* host = nullptr;
+  rc = rayt::unique_launch(dev, words, n, nib, unique, scratch, bytes - 256, counts, s, &host);
   if (rc != RAYT_OK) return rc;
-  *unique_count = host;
+  RAYT_CUDA_TRY(cudaStreamSynchronize(s));
+  if (host[1]) {
+    const int zero = 0;
+    cudaMemcpy(rayt::device_error_flag(), &zero, 4, cudaMemcpyHostToDevice);
+    return fail(RAYT_E_TIMEOUT, "a bounded device wait gave up (look-back did not complete)");
+  }
+  *unique_count = host[0];
   return RAYT_OK;
 }
 
