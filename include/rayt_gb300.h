@@ -350,8 +350,9 @@ int rayt_scan_i32(int32_t* device_data, int n, void* stream);
  * stream compaction, then, when the kept values span at most 32 per input
  * word and at most 2^26, a bitmap over their range read in order; otherwise
  * an LSD radix sort and unique.  The scratch memory is a device buffer the
- * library keeps per device and grows on demand.  device_words is not
- * modified. */
+ * library keeps per device and grows on demand.  The device work is captured
+ * once as a CUDA graph and replayed while the pointers, n and nodes_in_block
+ * repeat (one graph per device is kept).  device_words is not modified. */
 int rayt_feedback_unique(const int32_t* device_words, int n, int nodes_in_block,
                          int32_t* device_unique, int* unique_count, void* stream);
 
