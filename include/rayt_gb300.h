@@ -363,9 +363,12 @@ int rayt_feedback_unique(const int32_t* device_words, int n, int nodes_in_block,
  * cudaMalloc/cudaFree: its scratch is a fixed __device__ array of about
  * 17 MiB that each GPU loading the library keeps until exit, sized for n up
  * to RAYT_FEEDBACK_UNIQUE_NOALLOC_MAX_WORDS (larger n returns RAYT_E_LIMIT).
- * All calls on a device share that array: calls whose GPU work overlaps race,
- * so order them on one stream or synchronise in between.  The first call on a
- * device looks up the array's address; make it before any stream capture.
+ * All calls on a device share that array: calls whose GPU work overlaps race.
+ * The library serialises its own calls: this entry point, rayt_sort_i32,
+ * rayt_scan_i32 and rayt_feedback_unique take one lock and return after their
+ * stream finished (they share a device error flag and look-back epoch).  The
+ * first call on a device looks up the array's address and zeroes the array on
+ * `stream`; make it before any stream capture.
  * Returns after the result is on the device and *unique_count is set. */
 #define RAYT_FEEDBACK_UNIQUE_NOALLOC_MAX_WORDS (1 << 21)
 int rayt_feedback_unique_noalloc(const int32_t* device_words, int n, int nodes_in_block,
@@ -378,6 +381,15 @@ int rayt_feedback_unique_noalloc(const int32_t* device_words, int n, int nodes_i
  * word nothing ever publishes, with a limit of limit_s seconds, and returns
  * RAYT_OK when the wait gave up and was reported as it must. */
 int rayt_selftest_bounded_wait(double limit_s, void* stream);
+
+/* No counterpart in the reference.  Testing hook for the look-back epoch of
+ * the sort/unique kernels: their look-back words are tagged with a 27-bit
+ * per-call epoch, and before the epoch would repeat (after 2^27 - 1 calls on
+ * a device) the library clears every look-back table of the device and
+ * restarts it.  This sets the current device's epoch (and the library's count
+ * of calls since the last clear) to `calls`, so a test can make the restart
+ * happen within a few calls. */
+int rayt_testing_set_lookback_epoch(uint32_t calls);
 
 #ifdef __cplusplus
 }

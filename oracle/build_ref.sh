@@ -7,8 +7,11 @@
 #
 # The .cl kernels are copied into oracle/_ref/cl/ with one mechanical rewrite:
 # OpenCL vector literals "(float4)(a, b, c, d)" become "float4(a, b, c, d)".
+#
+#   RAYT_REFERENCE=<reference checkout> bash oracle/build_ref.sh
 set -euo pipefail
-REF="${RAYT_REFERENCE:-/root/reference}/rayt"
+[ -n "${RAYT_REFERENCE:-}" ] || { echo "set RAYT_REFERENCE to the reference checkout (the directory holding rayt/)" >&2; exit 3; }
+REF="$RAYT_REFERENCE/rayt"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 [ -d "$REF" ] || { echo "reference sources not found at $REF" >&2; exit 3; }

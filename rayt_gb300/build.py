@@ -71,10 +71,11 @@ def build_oracle(force=False):
 
 
 def build_reference_harness():
-    """Compiles the reference's own code into oracle/_ref (only where the
-    reference sources exist, i.e. the development container)."""
-    ref = os.environ.get("RAYT_REFERENCE", "/root/reference")
-    if not os.path.isdir(os.path.join(ref, "rayt")):
+    """Compiles the reference's own code into oracle/_ref when RAYT_REFERENCE
+    names a reference checkout (the directory holding rayt/); skipped
+    otherwise.  Only the golden-fixture generator uses it."""
+    ref = os.environ.get("RAYT_REFERENCE")
+    if not ref or not os.path.isdir(os.path.join(ref, "rayt")):
         return None
     _run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh")])
     return os.path.join(ROOT, "oracle", "_ref", "librayt_ref.so")

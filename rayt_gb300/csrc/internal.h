@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <mutex>
 #include <string>
 #include <vector>
 #include "../../include/rayt_gb300.h"
@@ -157,6 +158,25 @@ size_t scan_scratch_bytes(int n);
 cudaError_t scan_i32_device(int32_t* data, int n, void* scratch, size_t scratch_bytes, cudaStream_t s);
 // Device error flag set by bounded waits that gave up (decoupled look-back).
 int* device_error_flag();
+// The sort/unique look-back words carry the tag epoch * 8 + pass, where the
+// device-side epoch (27 bits) advances once per sort or unique call.  Sets
+// that epoch (stream-ordered on s).
+cudaError_t set_lookback_epoch(uint32_t epoch, cudaStream_t s);
+
+// ---- stand-alone primitives (prims.cpp) -------------------------------------------
+// Serialises every sort/scan/unique entry point on all devices: they share
+// the device error flag and the look-back epoch, and each one holds the lock
+// until its stream has finished its work.
+std::mutex& prims_mutex();
+// Called (with prims_mutex held) before each sort or unique call on the
+// current device: counts epochs, and before the epoch would repeat a tag
+// still present in a look-back table (after 2^27 - 1 calls), clears every
+// look-back table of the device on s and restarts the epoch at 0.
+int lookback_epoch_step(cudaStream_t s);
+// Registers a scratch area holding look-back tables on the current device
+// besides the library's growable scratch (the allocation-free entry point's
+// static array), so lookback_epoch_step clears it too.
+void register_lookback_area(void* p, size_t bytes);
 // Runs one wait on a word nothing publishes, with a limit of limit_s seconds
 // (restored to 1 s after); the wait must give up and set the error flag.
 cudaError_t bounded_wait_probe(double limit_s, cudaStream_t s);

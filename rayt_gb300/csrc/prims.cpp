@@ -1,7 +1,7 @@
 // C ABI of the stand-alone feedback primitives (GPUSort, GPUScan and the
 // feedback extractor's GetUnique).  Scratch memory is a per-device buffer the
-// library grows on demand and keeps; calls on one device are serialised by a
-// mutex, so concurrent host threads do not share it mid-operation.
+// library grows on demand and keeps; calls are serialised by one mutex, so
+// concurrent host threads do not share it mid-operation.
 #include <mutex>
 #include "internal.h"
 
@@ -11,10 +11,53 @@ struct Scratch {
   void* ptr = nullptr;
   size_t bytes = 0;
 };
-std::mutex g_mu;
 Scratch g_scratch[64];
 
-int get_scratch(size_t bytes, void** out) {
+// Look-back epoch bookkeeping per device: calls since the tables were last
+// cleared (= the device epoch), and the static area of the allocation-free
+// entry point.
+constexpr uint32_t kEpochLimit = (1u << 27) - 1;
+uint32_t g_epoch_calls[64];
+Scratch g_static_area[64];
+
+int current_device(int* dev) {
+  RAYT_CUDA_TRY(cudaGetDevice(dev));
+  if (*dev < 0 || *dev >= 64) return fail(RAYT_E_ARG, "device ordinal out of range");
+  return RAYT_OK;
+}
+}  // namespace
+
+std::mutex& prims_mutex() {
+  static std::mutex mu;
+  return mu;
+}
+
+void register_lookback_area(void* p, size_t bytes) {
+  int dev = 0;
+  if (current_device(&dev) != RAYT_OK) return;
+  g_static_area[dev].ptr = p;
+  g_static_area[dev].bytes = bytes;
+}
+
+int lookback_epoch_step(cudaStream_t s) {
+  int dev = 0;
+  int rc = current_device(&dev);
+  if (rc != RAYT_OK) return rc;
+  if (g_epoch_calls[dev] >= kEpochLimit) {
+    // the next epoch would reuse a tag that old look-back words may still
+    // carry: zero every table (a zero word is never "published") and restart
+    for (const Scratch* a : {&g_scratch[dev], &g_static_area[dev]})
+      if (a->ptr) RAYT_CUDA_TRY(cudaMemsetAsync(a->ptr, 0, a->bytes, s));
+    RAYT_CUDA_TRY(set_lookback_epoch(0, s));
+    g_epoch_calls[dev] = 0;
+  }
+  ++g_epoch_calls[dev];
+  return RAYT_OK;
+}
+
+namespace {
+
+int get_scratch(size_t bytes, void** out, cudaStream_t stream) {
   int dev = 0;
   RAYT_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return fail(RAYT_E_ARG, "device ordinal out of range");
@@ -28,8 +71,9 @@ int get_scratch(size_t bytes, void** out) {
     }
     if (cudaMalloc(&s.ptr, bytes) != cudaSuccess) return fail(RAYT_E_OOM, "scratch allocation failed");
     s.bytes = bytes;
-    // the sort's look-back words are epoch-tagged, never cleared: start from zeros
-    RAYT_CUDA_TRY(cudaMemset(s.ptr, 0, bytes));
+    // the sort's look-back words are epoch-tagged, never cleared: start from
+    // zeros, ordered before the call's kernels on the caller's stream
+    RAYT_CUDA_TRY(cudaMemsetAsync(s.ptr, 0, bytes, stream));
   }
   *out = s.ptr;
   return RAYT_OK;
@@ -105,12 +149,13 @@ int rayt_sort_i32(int32_t* data, int n, void* stream) {
   if (n < 0 || (n > 0 && !data)) return fail(RAYT_E_ARG, "rayt_sort_i32: bad arguments");
   if (n >= (1 << 30)) return fail(RAYT_E_LIMIT, "rayt_sort_i32: n must be below 2^30");
   if (n <= 1) return RAYT_OK;
-  std::lock_guard<std::mutex> lock(rayt::g_mu);
+  std::lock_guard<std::mutex> lock(rayt::prims_mutex());
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   void* scratch = nullptr;
   const size_t bytes = rayt::sort_scratch_bytes(n);
-  int rc = rayt::get_scratch(bytes, &scratch);
+  int rc = rayt::get_scratch(bytes, &scratch, s);
   if (rc != RAYT_OK) return rc;
+  if ((rc = rayt::lookback_epoch_step(s)) != RAYT_OK) return rc;
   RAYT_CUDA_TRY(rayt::sort_i32_device(data, n, scratch, bytes, s));
   return rayt::check_device_error(s);
 }
@@ -119,19 +164,31 @@ int rayt_scan_i32(int32_t* data, int n, void* stream) {
   if (n < 0 || (n > 0 && !data)) return fail(RAYT_E_ARG, "rayt_scan_i32: bad arguments");
   if (n >= (1 << 30)) return fail(RAYT_E_LIMIT, "rayt_scan_i32: n must be below 2^30");
   if (n == 0) return RAYT_OK;
-  std::lock_guard<std::mutex> lock(rayt::g_mu);
+  std::lock_guard<std::mutex> lock(rayt::prims_mutex());
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   void* scratch = nullptr;
   const size_t bytes = rayt::scan_scratch_bytes(n);
-  int rc = rayt::get_scratch(bytes, &scratch);
+  int rc = rayt::get_scratch(bytes, &scratch, s);
   if (rc != RAYT_OK) return rc;
   RAYT_CUDA_TRY(rayt::scan_i32_device(data, n, scratch, bytes, s));
   return rayt::check_device_error(s);
 }
 
+int rayt_testing_set_lookback_epoch(uint32_t calls) {
+  if (calls >= (1u << 27)) return fail(RAYT_E_ARG, "rayt_testing_set_lookback_epoch: epoch out of range");
+  std::lock_guard<std::mutex> lock(rayt::prims_mutex());
+  int dev = 0;
+  RAYT_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(RAYT_E_ARG, "device ordinal out of range");
+  RAYT_CUDA_TRY(rayt::set_lookback_epoch(calls, nullptr));
+  RAYT_CUDA_TRY(cudaDeviceSynchronize());
+  rayt::g_epoch_calls[dev] = calls;
+  return RAYT_OK;
+}
+
 int rayt_selftest_bounded_wait(double limit_s, void* stream) {
   if (!(limit_s > 0) || limit_s > 10) return fail(RAYT_E_ARG, "rayt_selftest_bounded_wait: limit out of range (0, 10] s");
-  std::lock_guard<std::mutex> lock(rayt::g_mu);
+  std::lock_guard<std::mutex> lock(rayt::prims_mutex());
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   RAYT_CUDA_TRY(rayt::bounded_wait_probe(limit_s, s));
   const int rc = rayt::check_device_error(s);
@@ -147,16 +204,17 @@ int rayt_feedback_unique(const int32_t* words, int n, int nib, int32_t* unique, 
     *unique_count = 0;
     return RAYT_OK;
   }
-  std::lock_guard<std::mutex> lock(rayt::g_mu);
+  std::lock_guard<std::mutex> lock(rayt::prims_mutex());
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   void* scratch = nullptr;
   const size_t bytes = rayt::feedback_scratch_bytes(n) + 256;
-  int rc = rayt::get_scratch(bytes, &scratch);
+  int rc = rayt::get_scratch(bytes, &scratch, s);
   if (rc != RAYT_OK) return rc;
   int* counts = reinterpret_cast<int*>(static_cast<uint8_t*>(scratch) + (bytes - 256));
   int dev = 0;
   RAYT_CUDA_TRY(cudaGetDevice(&dev));
   int* host = nullptr;
+  if ((rc = rayt::lookback_epoch_step(s)) != RAYT_OK) return rc;
   rc = rayt::unique_launch(dev, words, n, nib, unique, scratch, bytes - 256, counts, s, &host);
   if (rc != RAYT_OK) return rc;
   RAYT_CUDA_TRY(cudaStreamSynchronize(s));

@@ -1089,6 +1089,11 @@ int* device_error_flag() {
   return p;
 }
 
+cudaError_t set_lookback_epoch(uint32_t epoch, cudaStream_t s) {
+  // pageable source: the copy reads `epoch` before the call returns
+  return cudaMemcpyToSymbolAsync(g_epoch, &epoch, sizeof(epoch), 0, cudaMemcpyHostToDevice, s);
+}
+
 size_t sort_scratch_bytes(int n) { return layout(nullptr, n).bytes; }
 size_t feedback_scratch_bytes(int n) { return layout(nullptr, n).bytes; }
 size_t scan_scratch_bytes(int n) { return (((size_t)n + kTile - 1) / kTile + 1) * 8 + 256; }

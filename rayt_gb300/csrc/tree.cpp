@@ -149,32 +149,58 @@ M4 Transposed(const M4& a) {
   }
   return r;
 }
-// Inverse by Gauss-Jordan elimination with partial pivoting, in double
-// precision, rounded to float at the end.  (The reference inverts in float by
-// cofactors; the two can differ in the last bits, which is why parity runs
-// pass the reference's own 16 floats to rayt_render_frame.)
+// fmat4::Inverse (rayt/util/mat.cpp:20-107): the cofactor method of Intel's
+// published SSE 4x4-inverse note, in float with the reference's operation
+// order, so the 16 floats match the reference bit for bit.  With s the
+// transpose of the matrix, each cofactor is (three pair-products x s) minus
+// (three pair-products x s), each sum taken left to right; the pair products
+// of the first eight cofactors come from s's rows 2-3, those of the last eight
+// from rows 0-1.
+struct Cofactor {
+  uint8_t plus[3][2], minus[3][2];  // {pair product, s index}
+};
+constexpr uint8_t kPairsLo[12][2] = {{10, 15}, {11, 14}, {9, 15}, {11, 13}, {9, 14}, {10, 13},
+                                     {8, 15},  {11, 12}, {8, 14}, {10, 12}, {8, 13}, {9, 12}};
+constexpr uint8_t kPairsHi[12][2] = {{2, 7}, {3, 6}, {1, 7}, {3, 5}, {1, 6}, {2, 5},
+                                     {0, 7}, {3, 4}, {0, 6}, {2, 4}, {0, 5}, {1, 4}};
+constexpr Cofactor kCofactors[16] = {
+    {{{0, 5}, {3, 6}, {4, 7}}, {{1, 5}, {2, 6}, {5, 7}}},
+    {{{1, 4}, {6, 6}, {9, 7}}, {{0, 4}, {7, 6}, {8, 7}}},
+    {{{2, 4}, {7, 5}, {10, 7}}, {{3, 4}, {6, 5}, {11, 7}}},
+    {{{5, 4}, {8, 5}, {11, 6}}, {{4, 4}, {9, 5}, {10, 6}}},
+    {{{1, 1}, {2, 2}, {5, 3}}, {{0, 1}, {3, 2}, {4, 3}}},
+    {{{0, 0}, {7, 2}, {8, 3}}, {{1, 0}, {6, 2}, {9, 3}}},
+    {{{3, 0}, {6, 1}, {11, 3}}, {{2, 0}, {7, 1}, {10, 3}}},
+    {{{4, 0}, {9, 1}, {10, 2}}, {{5, 0}, {8, 1}, {11, 2}}},
+    {{{0, 13}, {3, 14}, {4, 15}}, {{1, 13}, {2, 14}, {5, 15}}},
+    {{{1, 12}, {6, 14}, {9, 15}}, {{0, 12}, {7, 14}, {8, 15}}},
+    {{{2, 12}, {7, 13}, {10, 15}}, {{3, 12}, {6, 13}, {11, 15}}},
+    {{{5, 12}, {8, 13}, {11, 14}}, {{4, 12}, {9, 13}, {10, 14}}},
+    {{{2, 10}, {5, 11}, {1, 9}}, {{4, 11}, {0, 9}, {3, 10}}},
+    {{{8, 11}, {0, 8}, {7, 10}}, {{6, 10}, {9, 11}, {1, 8}}},
+    {{{6, 9}, {11, 11}, {3, 8}}, {{10, 11}, {2, 8}, {7, 9}}},
+    {{{10, 10}, {4, 8}, {9, 9}}, {{8, 9}, {11, 10}, {5, 8}}},
+};
 M4 Inverse(const M4& a) {
-  double w[4][8];
-  for (int i = 0; i < 4; ++i)
-    for (int j = 0; j < 8; ++j) w[i][j] = j < 4 ? (double)a.m[i * 4 + j] : (j - 4 == i ? 1.0 : 0.0);
-  for (int col = 0; col < 4; ++col) {
-    int piv = col;
-    for (int r = col + 1; r < 4; ++r)
-      if (std::fabs(w[r][col]) > std::fabs(w[piv][col])) piv = r;
-    if (piv != col)
-      for (int j = 0; j < 8; ++j) std::swap(w[piv][j], w[col][j]);
-    const double inv = 1.0 / w[col][col];
-    for (int j = 0; j < 8; ++j) w[col][j] *= inv;
-    for (int r = 0; r < 4; ++r) {
-      if (r == col) continue;
-      const double f = w[r][col];
-      if (f == 0.0) continue;
-      for (int j = 0; j < 8; ++j) w[r][j] -= f * w[col][j];
-    }
+  const M4 s = Transposed(a);
+  float lo[12], hi[12];
+  for (int k = 0; k < 12; ++k) {
+    lo[k] = s.m[kPairsLo[k][0]] * s.m[kPairsLo[k][1]];
+    hi[k] = s.m[kPairsHi[k][0]] * s.m[kPairsHi[k][1]];
   }
   M4 r;
-  for (int i = 0; i < 4; ++i)
-    for (int j = 0; j < 4; ++j) r.m[i * 4 + j] = (float)w[i][4 + j];
+  for (int j = 0; j < 16; ++j) {
+    const float* pr = j < 8 ? lo : hi;
+    const Cofactor& c = kCofactors[j];
+    float v = pr[c.plus[0][0]] * s.m[c.plus[0][1]] + pr[c.plus[1][0]] * s.m[c.plus[1][1]] +
+              pr[c.plus[2][0]] * s.m[c.plus[2][1]];
+    v -= pr[c.minus[0][0]] * s.m[c.minus[0][1]] + pr[c.minus[1][0]] * s.m[c.minus[1][1]] +
+         pr[c.minus[2][0]] * s.m[c.minus[2][1]];
+    r.m[j] = v;
+  }
+  float det = s.m[0] * r.m[0] + s.m[1] * r.m[1] + s.m[2] * r.m[2] + s.m[3] * r.m[3];
+  det = 1.0f / det;
+  for (int j = 0; j < 16; ++j) r.m[j] *= det;
   return r;
 }
 }  // namespace

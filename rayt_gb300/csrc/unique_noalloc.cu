@@ -16,13 +16,18 @@
 //    RAYT_E_LIMIT before any GPU work.  The array is about 17 MiB and every
 //    GPU that loads the library holds it until the process exits.
 //  * Every call on a device uses the same array, so two calls whose GPU work
-//    overlaps (different streams, or different host threads without ordering)
-//    race and both results are undefined.  Order them on one stream or
-//    synchronise between them.  The array keeps the previous call's contents;
+//    overlaps race and both results are undefined.  Calls through this entry
+//    point take the library's primitives lock and return only after their
+//    stream has finished, so calls from several host threads are serialised
+//    like rayt_sort_i32 / rayt_scan_i32 / rayt_feedback_unique, with which
+//    they also share the device error flag and the look-back epoch.  GPU work
+//    the caller queued on other streams that reads or writes the array is not
+//    ordered by the library.  The array keeps the previous call's contents;
 //    every part the kernels expect to start at zero is cleared by each call.
 //  * The first call on each device looks up the array's device address with
-//    cudaGetSymbolAddress and zeroes it once (with that device current); make
-//    that first call before any stream capture.
+//    cudaGetSymbolAddress (with that device current) and zeroes the array on
+//    the caller's stream, ordered before that call's kernels; make that first
+//    call before any stream capture.
 // No cudaMalloc, cudaFree or allocating library routine is called here.
 #include <mutex>
 
@@ -48,20 +53,22 @@ constexpr size_t kScratchBytes = 2 * Up256((size_t)kMaxWords * 4 + 16) + Up256(6
 
 static __device__ __align__(256) uint8_t g_noalloc_scratch[kScratchBytes + kCountsBytes];
 
-std::mutex g_setup_mu;
 void* g_scratch_ptr[64];
 
-// Device address of g_noalloc_scratch on the current device (looked up once).
-int scratch_address(void** out) {
+// Device address of g_noalloc_scratch on the current device (looked up once;
+// the caller holds prims_mutex()).  The first lookup zeroes the array on the
+// caller's stream s, so the zeroing is ordered before that call's kernels even
+// when s does not synchronise with the legacy default stream.
+int scratch_address(void** out, cudaStream_t s) {
   int dev = 0;
   RAYT_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return fail(RAYT_E_ARG, "device ordinal out of range");
-  std::lock_guard<std::mutex> lock(g_setup_mu);
   if (!g_scratch_ptr[dev]) {
     void* p = nullptr;
     RAYT_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
     // the sort's look-back words are epoch-tagged, never cleared: start from zeros
-    RAYT_CUDA_TRY(cudaMemset(p, 0, sizeof(g_noalloc_scratch)));
+    RAYT_CUDA_TRY(cudaMemsetAsync(p, 0, sizeof(g_noalloc_scratch), s));
+    register_lookback_area(p, sizeof(g_noalloc_scratch));
     g_scratch_ptr[dev] = p;
   }
   *out = g_scratch_ptr[dev];
@@ -84,10 +91,12 @@ extern "C" int rayt_feedback_unique_noalloc(const int32_t* words, int n, int nod
   }
   if (rayt::feedback_scratch_bytes(n) > rayt::kScratchBytes)
     return fail(RAYT_E_LIMIT, "rayt_feedback_unique_noalloc: scratch layout larger than the static area");
-  void* base = nullptr;
-  int rc = rayt::scratch_address(&base);
-  if (rc != RAYT_OK) return rc;
+  std::lock_guard<std::mutex> lock(rayt::prims_mutex());
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  void* base = nullptr;
+  int rc = rayt::scratch_address(&base, s);
+  if (rc != RAYT_OK) return rc;
+  if ((rc = rayt::lookback_epoch_step(s)) != RAYT_OK) return rc;
   int* counts = reinterpret_cast<int*>(static_cast<uint8_t*>(base) + rayt::kScratchBytes);
   // the launcher clears the histograms, tile counters and counts it relies on
   RAYT_CUDA_TRY(rayt::feedback_unique_device(words, n, nodes_in_block, unique, counts, base, rayt::kScratchBytes, s));

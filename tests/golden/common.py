@@ -30,6 +30,41 @@ def canonical_tree_bytes(path):
     return bytes(b)
 
 
+def canonical_tree_sha(path, chunk_blocks=4096):
+    """(sha256, bytes) of canonical_tree_bytes(path), streamed block by block
+    so multi-GB files need not fit in memory."""
+    h = hashlib.sha256()
+    size = 0
+    with open(path, "rb") as f:
+        head = f.read(20)
+        nib, blocks, root, stride, nch = np.frombuffer(head, "<u4")
+        rest = b""
+        for _ in range(int(nch)):
+            rec = f.read(8)
+            ln = int.from_bytes(rec[4:8], "little")
+            rest += rec + f.read(ln)
+        h.update(head + rest)
+        size += len(head) + len(rest)
+        stride = int(stride)
+        left = int(blocks)
+        while left:
+            k = min(left, chunk_blocks)
+            buf = np.frombuffer(f.read(stride * k), np.uint8).copy()
+            if buf.size != stride * k:
+                raise ValueError("truncated tree file")
+            rec = buf.reshape(k, stride)
+            rc = rec[:, 8:12].copy().view("<u4").ravel()
+            for r in range(8):
+                rec[rc <= r, 12 + 8 * r:20 + 8 * r] = 0
+            h.update(rec.tobytes())
+            size += rec.size
+            left -= k
+        tail = f.read()
+        h.update(tail)
+        size += len(tail)
+    return h.hexdigest(), size
+
+
 def _terrain(depth, spheres=0, min_radius=8, max_radius=256, seed=1, sphere_seed=2):
     return {"depth": depth, "seed": seed, "base_cells": 4, "octaves": 6, "spheres": spheres,
             "sphere_seed": sphere_seed, "min_radius": min_radius, "max_radius": max_radius}
@@ -44,6 +79,34 @@ BUILDER_CASES = {
     "terrain8s": {"kind": "terrain", "terrain": _terrain(8, spheres=60, min_radius=2, max_radius=24), "nib": 512},
     "terrain10": {"kind": "terrain", "terrain": _terrain(10), "nib": 4096},
 }
+
+# The benchmark scenes (1080p flythrough and 64-view workloads: depth 12, the
+# fBm heightfield plus 2000 sphere shells of radius 8..256 voxels, 4096-node
+# blocks).  Too large to commit or to build in the CPU tests: the golden file
+# keeps the canonical hash of the reference builder's output, and the GPU
+# tests compare the product builder's file with it.
+LARGE_BUILDER_CASES = {
+    "terrain12s": {"kind": "terrain", "terrain": _terrain(12, spheres=2000, min_radius=8, max_radius=256),
+                   "nib": 4096},
+}
+
+# Camera::ViewProjectionMatrix().Inverse() over a seeded sweep of cameras.
+CAMERA_SWEEP = {"count": 512, "seed": 5}
+
+
+def camera_sweep(count, seed):
+    """count x 8 float32: yaw, pitch, roll, x, y, z, horizontal fov, aspect."""
+    rng = np.random.default_rng(seed)
+    out = np.zeros((count, 8), np.float32)
+    out[:, 0] = rng.uniform(-360, 360, count)
+    out[:, 1] = rng.uniform(-90, 90, count)
+    out[:, 2] = rng.uniform(-180, 180, count)
+    out[:, 3:6] = rng.uniform(-1, 2, (count, 3))
+    out[:, 6] = rng.uniform(20, 120, count)
+    wh = rng.integers(1, 4096, (count, 2))
+    out[:, 7] = wh[:, 0] / wh[:, 1]
+    return out
+
 
 # Cache contents after InitialFillCache (the reference's OctreeGPUTest /
 # TestBuilder checks, stored-octree-test.cpp:212-233).

@@ -222,3 +222,51 @@ def test_bounded_wait_gives_up_and_context_survives(built):
     x = dev(a)
     R.GPUSort(x, a.size)
     np.testing.assert_array_equal(host(x), np.sort(a))
+
+
+def test_feedback_unique_cached_graph_replays(built):
+    """rayt_feedback_unique replays its cached graph while the pointers, n and
+    nodes_in_block repeat.  The same input and output buffers, refilled
+    between calls so the bitmap and radix paths alternate: every result equals
+    numpy's, so nothing of one call (path choice, counts) is baked in."""
+    import torch
+    n, nib = 300_000, 512
+    w = torch.zeros(n, dtype=torch.int32, device="cuda")
+    out = torch.zeros(n, dtype=torch.int32, device="cuda")
+    rng = np.random.default_rng(41)
+    paths = []
+    for k in range(8):
+        if k % 2 == 0:  # narrow keys: bitmap path
+            words = feedback_words(n, 100 + k, id_bits=14)
+        else:  # keys over the whole int32 range: radix passes
+            words = rng.integers(-2**31, 2**31 - 1, n, dtype=np.int64).astype(np.int32)
+            words[rng.random(n) < 0.6] = NO_HIT
+            words[:500] = words[500:1000]
+        paths.append(_bitmap_path(words, nib))
+        w.copy_(torch.from_numpy(words))
+        cnt = R.feedback_unique(w, n, nib, out)
+        np.testing.assert_array_equal(host(out)[:cnt], _np_unique(words, nib), err_msg="call %d" % k)
+    assert paths == [True, False] * 4
+
+
+def test_lookback_epoch_restart(built):
+    """The sort/unique look-back tags carry a 27-bit per-call epoch; before it
+    would repeat, every look-back table of the device is cleared and the epoch
+    restarts.  Driven to the restart through the testing hook: sorts and
+    feedback uniques across it stay exact, and so does a large call after a
+    run of small ones (whose stale look-back words a repeated tag would read)."""
+    import torch
+    L = R.lib()
+    big = feedback_words(1 << 22, 9, id_bits=30)  # wide: radix passes over many tiles
+    small = feedback_words(5000, 10)
+    try:
+        assert L.rayt_testing_set_lookback_epoch((1 << 27) - 4) == 0
+        for k in range(8):
+            words = big if k in (0, 7) else small
+            np.testing.assert_array_equal(_unique(words, 4096), _np_unique(words, 4096), err_msg="call %d" % k)
+            a = np.random.default_rng(k).integers(-2**31, 2**31 - 1, 70000, dtype=np.int64).astype(np.int32)
+            x = dev(a)
+            R.GPUSort(x, a.size)
+            np.testing.assert_array_equal(host(x), np.sort(a), err_msg="sort %d" % k)
+    finally:
+        torch.cuda.synchronize()

@@ -96,14 +96,29 @@ def test_terrain_with_spheres_is_deterministic(built, tmp_path):
     assert R.build_terrain(str(b), 7, 1024)[1] < na[1]  # spheres add nodes
 
 
-def test_camera_helper_close_to_reference(golden):
-    """The product's camera helper inverts in double precision; the reference
-    inverts in float, so agreement is to float rounding, not bit for bit."""
+def test_camera_helper_matches_reference(golden):
+    """The camera helper builds the reference's float matrix and inverts it with
+    the reference's float cofactor method: the 16 floats of every golden frame
+    camera are the reference's own, bit for bit."""
     from tests.golden.common import FRAME_CASES
     for name, case in FRAME_CASES.items():
         w, h = case["size"]
         for cam, g in zip(case["cameras"], golden["frames"][name]):
             c = R.Camera(cam[0], cam[1], cam[2], cam[3:6], cam[6], w / h)
-            m = c.view_proj_inv()
+            m = np.asarray(c.view_proj_inv(), np.float32)
             ref = np.array(g["matrix"], np.float32)
-            np.testing.assert_allclose(m, ref, rtol=2e-5, atol=2e-6)
+            np.testing.assert_array_equal(m.view(np.uint32), ref.view(np.uint32))
+
+
+def test_camera_helper_sweep_matches_reference():
+    """512 seeded cameras (any yaw/roll, pitch -90..90, FOV 20..120, aspect
+    from 1..4095-pixel sides) against Camera::ViewProjectionMatrix().Inverse()
+    run by the reference harness: bit for bit."""
+    from tests.golden.common import CAMERA_SWEEP, camera_sweep
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "cameras.npz"))
+    cams = camera_sweep(CAMERA_SWEEP["count"], CAMERA_SWEEP["seed"])
+    np.testing.assert_array_equal(cams, d["cameras"])
+    got = np.zeros_like(d["matrices"])
+    for i, c in enumerate(cams):
+        got[i] = R.Camera(c[0], c[1], c[2], c[3:6], c[6], c[7]).view_proj_inv()
+    np.testing.assert_array_equal(got.view(np.uint32), d["matrices"].view(np.uint32))
