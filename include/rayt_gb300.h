@@ -214,6 +214,29 @@ int rayt_renderer_read_image(rayt_renderer* r, void* host_rgba, size_t bytes);
  * follow one another in view order. */
 int rayt_renderer_pass_words(rayt_renderer* r, int pass, int32_t* host_words, size_t count);
 
+/* Depth and hit-node output (no counterpart in the reference, which keeps the
+ * hit distance only inside a pass: raytracing_pass.cl:43,50-51,
+ * raycast.cl:157-163).  Off by default; when on, every frame also writes per
+ * pixel (same layout as the image, row 0 at the bottom):
+ *   depth     float: the distance along the (normalised) ray direction from
+ *             the camera to what the pixel shows, in octree units (the octree
+ *             is the unit cube): the t at which each earlier pass stopped the
+ *             ray on a fault, plus the final hit's t, summed in float in pass
+ *             order.  +inf for a miss, NaN for an error (the iteration limit,
+ *             shown red).  A ray still faulted when the frame ends (shaded
+ *             with its fault's parent node) gets the distance where it stopped.
+ *   hit node  int32: the cache node index (slot * nodes_in_block + node) that
+ *             shaded the pixel - the hit node, or the fault's parent node for a
+ *             ray still faulted at the end - -1 for a miss, -2 for an error.
+ * Turning it on allocates both buffers (and 4 bytes per ray record). */
+int rayt_renderer_set_depth_output(rayt_renderer* r, int on);
+/* Device pointers of view `view`'s depth (float) and hit-node (int32) buffers;
+ * either out pointer may be NULL.  RAYT_E_STATE if depth output was never on. */
+int rayt_renderer_depth(rayt_renderer* r, int view, void** device_depth, void** device_hit_nodes);
+/* Copies view `view`'s depth and/or hit nodes (count >= its pixels) to host
+ * memory; either host pointer may be NULL. */
+int rayt_renderer_read_depth(rayt_renderer* r, int view, float* host_depth, int32_t* host_hit_nodes, size_t count);
+
 /* Batched form (no counterpart in the reference, which renders one view per
  * RenderFrame).  A renderer over n_views views (1..512) of any sizes; each
  * frame traces all views in the same persistent launches and one cache

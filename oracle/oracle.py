@@ -41,6 +41,7 @@ def lib():
             "oracle_render_frame": (i32, [vp, C.POINTER(C.c_float)]),
             "oracle_frame_image": (i32, [vp, vp]),
             "oracle_frame_pass_words": (i32, [vp, i32, vp]),
+            "oracle_frame_depth": (i32, [vp, vp, vp]),
             "oracle_renderer_counters": (None, [vp, C.POINTER(C.c_longlong)]),
             "oracle_trace_once": (i32, [vp, C.POINTER(C.c_float), vp, vp]),
             "oracle_depth_view": (i32, [vp, C.POINTER(C.c_float), C.c_float, i32, i32, vp]),
@@ -119,6 +120,21 @@ class OracleScene:
         out = np.zeros(sum(a * b for a, b in self.views) if self.views else self.w * self.h, np.int32)
         if lib().oracle_frame_pass_words(self.r, i, out.ctypes.data) != 0:
             raise IndexError(i)
+        return out
+
+    def depth(self):
+        """(depth, hit node) of the last frame: one (h, w) pair per view (a
+        single pair without views)."""
+        n = sum(a * b for a, b in self.views) if self.views else self.w * self.h
+        depth = np.zeros(n, np.float32)
+        nodes = np.zeros(n, np.int32)
+        lib().oracle_frame_depth(self.r, depth.ctypes.data, nodes.ctypes.data)
+        if not self.views:
+            return depth.reshape(self.h, self.w), nodes.reshape(self.h, self.w)
+        out, o = [], 0
+        for w, h in self.views:
+            out.append((depth[o:o + w * h].reshape(h, w), nodes[o:o + w * h].reshape(h, w)))
+            o += w * h
         return out
 
     def trace_once(self, mat):

@@ -343,7 +343,15 @@ struct RayState {
   int fault_parent;
   uint8_t color[4];
   uint8_t mult[4];
+  // Depth output (no reference counterpart): the distance the ray advanced
+  // over faulted passes (the t of each fault, summed in float in pass order),
+  // and the pixel's final depth and shading node.
+  float adv;
+  float depth;
+  int node;
 };
+constexpr uint32_t kDepthNaN = 0x7fffffffu, kDepthInf = 0x7f800000u;
+inline float FloatBits(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
 
 // init_tracing_frame.cl:11-45
 void InitRay(RayState& s, int x, int y, int W, int H, const float* m, float lod) {
@@ -360,6 +368,9 @@ void InitRay(RayState& s, int x, int y, int W, int H, const float* m, float lod)
   s.fault_parent = -1;
   std::memset(s.color, 0, 4);
   std::memset(s.mult, 255, 4);
+  s.adv = 0.0f;
+  s.depth = FloatBits(kDepthInf);
+  s.node = -1;
 }
 
 struct CastResult {
@@ -561,6 +572,8 @@ int32_t TracePixel(RayState& s, const Cache& c, const uint32_t* links, const int
   if (res->error) {
     s.color[0] = 255; s.color[1] = 0; s.color[2] = 0; s.color[3] = 255;
     std::memset(s.mult, 0, 4);
+    s.depth = FloatBits(kDepthNaN);
+    s.node = -2;
     return kNoHit;
   }
   if (res->fault_block != -1) {
@@ -569,19 +582,28 @@ int32_t TracePixel(RayState& s, const Cache& c, const uint32_t* links, const int
     s.origin.z = s.origin.z + s.dir.z * res->t;
     s.origin.w = s.origin.w + s.dir.w * res->t;
     s.fault_parent = res->node;
+    s.adv = s.adv + res->t;
     return -res->fault_block - 1;
   }
   if (res->node == -1) {
     std::memset(s.mult, 0, 4);
+    s.depth = FloatBits(kDepthInf);
+    s.node = -1;
     return kNoHit;
   }
   if (normals && colors) Shade(res->node, s, normals, colors);
   else std::memset(s.mult, 0, 4);
+  s.depth = s.adv + res->t;
+  s.node = res->node;
   return (int32_t)(((uint32_t)(res->node + 1) << 1) | (uint32_t)res->dup);
 }
 
 // finish_tracing_frame.cl:3-24
 void FinishPixel(RayState& s, const int8_t* normals, const uint8_t* colors, uint8_t* out) {
+  if (!Done(s)) {  // still faulted: the parent's colour at the distance where the ray stopped
+    s.depth = s.adv;
+    s.node = s.fault_parent;
+  }
   if (!Done(s) && normals && colors) Shade(s.fault_parent, s, normals, colors);
   const float bg[4] = {0.0f, (float)(216 / 255.), 1.0f, 1.0f};
   for (int k = 0; k < 4; ++k) {
@@ -913,6 +935,16 @@ int oracle_render_frame(void* rp, const float* view_proj_inv) {
 int oracle_frame_image(void* rp, unsigned char* out) {
   Renderer* r = static_cast<Renderer*>(rp);
   std::memcpy(out, r->image.data(), r->image.size());
+  return 0;
+}
+// Depth output of the last frame: per pixel (views concatenated in order) the
+// distance to what it shows and the cache node that shaded it.
+int oracle_frame_depth(void* rp, float* depth, int* nodes) {
+  Renderer* r = static_cast<Renderer*>(rp);
+  for (size_t i = 0; i < r->total; ++i) {
+    if (depth) depth[i] = r->st[i].depth;
+    if (nodes) nodes[i] = r->st[i].node;
+  }
   return 0;
 }
 int oracle_frame_pass_words(void* rp, int pass, int* out) {

@@ -142,6 +142,9 @@ def lib():
         "rayt_renderer_stream": (i32, [vp, C.POINTER(vp)]),
         "rayt_renderer_read_image": (i32, [vp, vp, C.c_size_t]),
         "rayt_renderer_pass_words": (i32, [vp, i32, vp, C.c_size_t]),
+        "rayt_renderer_set_depth_output": (i32, [vp, i32]),
+        "rayt_renderer_depth": (i32, [vp, i32, C.POINTER(vp), C.POINTER(vp)]),
+        "rayt_renderer_read_depth": (i32, [vp, i32, C.POINTER(f32), C.POINTER(i32), C.c_size_t]),
         "rayt_renderer_stats": (i32, [vp, C.POINTER(FrameStats)]),
         "rayt_renderer_count_fetches": (i32, [vp, C.POINTER(f32), C.POINTER(C.c_int64)]),
         "rayt_renderer_time_pass": (i32, [vp, C.POINTER(f32), i32, C.POINTER(f32)]),
@@ -472,6 +475,26 @@ class GPURayTracer:
         out = np.zeros(sum(w * h for w, h in self.sizes), np.int32)
         _check(lib().rayt_renderer_pass_words(self._h, p, out.ctypes.data, out.size))
         return out
+
+    def set_depth_output(self, on=True):
+        """Per-pixel depth and hit-node buffers from the next frame on (see
+        rayt_renderer_set_depth_output)."""
+        _check(lib().rayt_renderer_set_depth_output(self._h, 1 if on else 0))
+
+    def read_depth(self, view=0):
+        """(depth float32 [h, w], hit node int32 [h, w]) of the last frame."""
+        w, h = self.sizes[view]
+        depth = np.zeros((h, w), np.float32)
+        nodes = np.zeros((h, w), np.int32)
+        _check(lib().rayt_renderer_read_depth(self._h, view, depth.ctypes.data_as(C.POINTER(C.c_float)),
+                                              nodes.ctypes.data_as(C.POINTER(C.c_int32)), w * h))
+        return depth, nodes
+
+    def depth_device_ptrs(self, view=0):
+        """Device pointers (depth, hit nodes) of a view."""
+        d, n = C.c_void_p(), C.c_void_p()
+        _check(lib().rayt_renderer_depth(self._h, view, C.byref(d), C.byref(n)))
+        return d.value, n.value
 
     def stats(self):
         s = FrameStats()

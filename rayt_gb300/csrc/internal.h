@@ -82,6 +82,13 @@ struct TraceParams {
   int* out_parent;
   uint32_t* out_ray;
   int* n_out;
+  // optional depth output (all four set, or all null): per pixel the distance
+  // along the ray to what it shows and the cache node that shaded it; records
+  // carry the distance a faulted ray advanced so far
+  float* depth;
+  int32_t* hit_node;
+  const float* in_adv;
+  float* out_adv;
   // feedback
   uint32_t* fault_bits;    // one bit per tree block
   int fault_bit_limit;     // number of tree blocks (bits in fault_bits)
@@ -108,6 +115,7 @@ struct RayList {
   float4* dir = nullptr;     // xyz direction, w LOD coefficient
   int* parent = nullptr;     // node the ray faulted under
   uint32_t* ray = nullptr;   // pixel index in the image buffer
+  float* adv = nullptr;      // distance advanced over earlier passes (depth output only)
 };
 
 // first: rays come from the views' cameras (refill = 32: one thread per ray

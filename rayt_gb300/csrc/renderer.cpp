@@ -36,6 +36,9 @@ class Renderer {
   int Autotune(const float* m, int reps, int* best);
   int ReadImage(int view, void* host, size_t bytes);
   int PassWords(int pass, int32_t* host, size_t count) const;
+  int SetDepthOutput(bool on);
+  int DepthBuffers(int view, float** depth, int32_t** nodes) const;
+  int ReadDepth(int view, float* depth, int32_t* nodes, size_t count);
 
   double time_limit = 1.0;  // the reference's default (gpu-ray-tracer.cpp:30-31)
   float lod = 1.5f;         // lod_voxel_size set by the caller
@@ -71,6 +74,9 @@ class Renderer {
   uchar4* d_images_ = nullptr;      // every view's image at its pix_base
   int32_t* d_dense_ = nullptr;      // recorded feedback words, same layout
   float* d_coords_ = nullptr;       // every view's pixel_coords()
+  bool depth_out_ = false;          // depth output on: the two buffers below and the lists' adv arrays
+  float* d_depth_ = nullptr;        // per pixel (same layout as the images): distance to what it shows
+  int32_t* d_hit_ = nullptr;        // per pixel: the cache node that shaded it (-1 miss, -2 error)
   RayList lists_[2];
   // [pass block 0][fault bits][hit bits][pass block 1]: pass k clears its own
   // block and the bitmaps with one memset and reads the other block's ray
@@ -134,7 +140,10 @@ Renderer::~Renderer() {
     cudaFree(l.dir);
     cudaFree(l.parent);
     cudaFree(l.ray);
+    cudaFree(l.adv);
   }
+  cudaFree(d_depth_);
+  cudaFree(d_hit_);
   cudaFree(d_dense_);
   cudaFree(d_state_);
   cudaFree(d_fetch_);
@@ -260,6 +269,12 @@ TraceParams Renderer::Params(int it) const {
   p.out_parent = out.parent;
   p.out_ray = out.ray;
   p.n_out = block(k) + 1;
+  if (depth_out_) {
+    p.depth = d_depth_;
+    p.hit_node = d_hit_;
+    p.in_adv = in.adv;
+    p.out_adv = out.adv;
+  }
   p.fault_bits = reinterpret_cast<uint32_t*>(d_state_ + kBlockInts);
   p.fault_bit_limit = (int)cache_->tree_blocks();
   p.hit_bits = reinterpret_cast<uint32_t*>(d_state_ + kBlockInts + fault_words_);
@@ -512,6 +527,7 @@ int Renderer::Frame(const float* m) {
   f.in_dir = p.out_dir;
   f.in_parent = p.out_parent;
   f.in_ray = p.out_ray;
+  f.in_adv = p.out_adv;
   f.n_in = p.n_out;
   RAYT_CUDA_TRY(launch_finish(f, active_prev, s_));
   if (active_prev > 0) ++launches;
@@ -619,6 +635,44 @@ int Renderer::PassWords(int pass, int32_t* host, size_t count) const {
   if (pass < 0 || pass >= (int)pass_words_.size()) return fail(RAYT_E_ARG, "no recorded pass with that index");
   if (count < pass_words_[pass].size()) return fail(RAYT_E_ARG, "word buffer too small");
   std::memcpy(host, pass_words_[pass].data(), pass_words_[pass].size() * 4);
+  return RAYT_OK;
+}
+
+// Depth output buffers (allocated on first use, kept while the renderer
+// lives): per-pixel distance and shading node, and the distance each faulted
+// ray has advanced, carried on its record between passes.
+int Renderer::SetDepthOutput(bool on) {
+  if (on && !d_depth_) {
+    const size_t n = (size_t)total_pixels_;
+    if (cudaMalloc(&d_depth_, (size_t)padded_pixels_ * 4) != cudaSuccess ||
+        cudaMalloc(&d_hit_, (size_t)padded_pixels_ * 4) != cudaSuccess ||
+        cudaMalloc(&lists_[0].adv, n * 4) != cudaSuccess || cudaMalloc(&lists_[1].adv, n * 4) != cudaSuccess)
+      return fail(RAYT_E_OOM, "depth output allocation failed");
+    RAYT_CUDA_TRY(cudaMemsetAsync(d_depth_, 0, (size_t)padded_pixels_ * 4, s_));
+    RAYT_CUDA_TRY(launch_fill_i32(d_hit_, -1, (size_t)padded_pixels_, s_));
+  }
+  depth_out_ = on;
+  return RAYT_OK;
+}
+
+int Renderer::DepthBuffers(int view, float** depth, int32_t** nodes) const {
+  if (view < 0 || view >= n_views()) return fail(RAYT_E_ARG, "view index out of range");
+  if (!d_depth_) return fail(RAYT_E_STATE, "depth output was never turned on");
+  if (depth) *depth = d_depth_ + views_[view].pix_base;
+  if (nodes) *nodes = d_hit_ + views_[view].pix_base;
+  return RAYT_OK;
+}
+
+int Renderer::ReadDepth(int view, float* depth, int32_t* nodes, size_t count) {
+  float* dd = nullptr;
+  int32_t* dn = nullptr;
+  int rc = DepthBuffers(view, &dd, &dn);
+  if (rc != RAYT_OK) return rc;
+  const size_t n = (size_t)views_[view].width * views_[view].height;
+  if (count < n) return fail(RAYT_E_ARG, "depth buffer too small");
+  if (depth) RAYT_CUDA_TRY(cudaMemcpyAsync(depth, dd, n * 4, cudaMemcpyDeviceToHost, s_));
+  if (nodes) RAYT_CUDA_TRY(cudaMemcpyAsync(nodes, dn, n * 4, cudaMemcpyDeviceToHost, s_));
+  RAYT_CUDA_TRY(cudaStreamSynchronize(s_));
   return RAYT_OK;
 }
 
@@ -760,6 +814,24 @@ int rayt_renderer_read_image(rayt_renderer* r, void* host, size_t bytes) {
 int rayt_renderer_pass_words(rayt_renderer* r, int pass, int32_t* host, size_t count) {
   if (!r || !host) return fail(RAYT_E_ARG, "null argument");
   return R(r)->PassWords(pass, host, count);
+}
+int rayt_renderer_set_depth_output(rayt_renderer* r, int on) {
+  if (!r) return fail(RAYT_E_ARG, "null renderer");
+  return R(r)->SetDepthOutput(on != 0);
+}
+int rayt_renderer_depth(rayt_renderer* r, int view, void** device_depth, void** device_hit_nodes) {
+  if (!r || (!device_depth && !device_hit_nodes)) return fail(RAYT_E_ARG, "null argument");
+  float* d = nullptr;
+  int32_t* n = nullptr;
+  const int rc = R(r)->DepthBuffers(view, &d, &n);
+  if (rc != RAYT_OK) return rc;
+  if (device_depth) *device_depth = d;
+  if (device_hit_nodes) *device_hit_nodes = n;
+  return RAYT_OK;
+}
+int rayt_renderer_read_depth(rayt_renderer* r, int view, float* host_depth, int32_t* host_hit_nodes, size_t count) {
+  if (!r || (!host_depth && !host_hit_nodes)) return fail(RAYT_E_ARG, "null argument");
+  return R(r)->ReadDepth(view, host_depth, host_hit_nodes, count);
 }
 int rayt_renderer_stats(const rayt_renderer* r, rayt_frame_stats* out) {
   if (!r || !out) return fail(RAYT_E_ARG, "null argument");

@@ -544,10 +544,13 @@ __device__ __forceinline__ bool first_pass_pixel(const TraceParams& p, int r, in
 // lanes once `refill` of them are idle; otherwise a warp takes new rays once
 // all 32 ended.
 // Ray r of the launch (first pass: tile r / 32 of the views; later passes:
-// record r of the input list): its pixel, origin and direction; false for
-// the lanes of a partial tile that fall outside their view.
+// record r of the input list): its pixel, origin, direction and (depth
+// output) the distance it advanced in earlier passes; false for the lanes of
+// a partial tile that fall outside their view.
 template <bool kFirst>
-__device__ __forceinline__ bool ray_at(const TraceParams& p, int r, uint32_t& ray, float4& o, float4& d) {
+__device__ __forceinline__ bool ray_at(const TraceParams& p, int r, uint32_t& ray, float4& o, float4& d,
+                                       float& adv) {
+  adv = 0.0f;
   if (kFirst) {
     int v, x, y;
     if (!first_pass_pixel(p, r, v, x, y)) return false;
@@ -558,9 +561,21 @@ __device__ __forceinline__ bool ray_at(const TraceParams& p, int r, uint32_t& ra
     o = p.in_origin[r];
     d = p.in_dir[r];
     ray = p.in_ray[r];
+    if (p.in_adv) adv = p.in_adv[r];
   }
   return true;
 }
+
+// Depth output of a pixel whose ray ended: the distance along the ray to what
+// the pixel shows (earlier passes' advances plus this pass's t, in float, in
+// pass order) and the cache node that shaded it.  Miss: +inf and -1; error
+// (iteration limit, corrupt cache): NaN and -2.
+__device__ __forceinline__ void write_depth(const TraceParams& p, uint32_t ray, float depth, int node) {
+  p.depth[ray] = depth;
+  p.hit_node[ray] = node;
+}
+constexpr uint32_t kDepthNaN = 0x7fffffffu;
+constexpr uint32_t kDepthInf = 0x7f800000u;
 
 // RaytracingPass's handling of an ended ray (raytracing_pass.cl:20-58) plus
 // FinishTracingFrame for rays that end here: the final pixel, the next pass's
@@ -568,7 +583,7 @@ __device__ __forceinline__ bool ray_at(const TraceParams& p, int r, uint32_t& ra
 // lanes whose rays ended, together.
 template <bool kCount>
 __device__ __forceinline__ void end_ray(const TraceParams& p, const RayEnd& e, uint32_t ray, float4 o, const float4 d,
-                                        uint32_t fetches, uint32_t far_fetches) {
+                                        float adv, uint32_t fetches, uint32_t far_fetches) {
   const int lane = threadIdx.x & 31;
   const bool faulted = !e.error && e.fault_block != -1;
   const bool hit = !e.error && e.fault_block == -1 && e.node != -1;
@@ -576,14 +591,17 @@ __device__ __forceinline__ void end_ray(const TraceParams& p, const RayEnd& e, u
   int32_t word = kNoHit;
   if (e.error) {
     p.image[ray] = finish(p, make_uchar4(255, 0, 0, 255));
+    if (p.depth) write_depth(p, ray, __uint_as_float(kDepthNaN), -2);
   } else if (faulted) {
     word = -fault_block - 1;
   } else if (!hit) {
     p.image[ray] = finish(p, make_uchar4(0, 0, 0, 0));
+    if (p.depth) write_depth(p, ray, __uint_as_float(kDepthInf), -1);
   } else {
     const uchar4 col = (p.normals && p.colors) ? shade(p, node) : make_uchar4(0, 0, 0, 0);
     p.image[ray] = finish(p, col);
     word = (int32_t)(((uint32_t)(node + 1) << 1) | (uint32_t)dup);
+    if (p.depth) write_depth(p, ray, adv + e.t, node);
   }
   if (p.words_dense) p.words_dense[ray] = word;
   const int slot = warp_append(p.n_out, faulted);
@@ -599,6 +617,7 @@ __device__ __forceinline__ void end_ray(const TraceParams& p, const RayEnd& e, u
     p.out_dir[slot] = d;
     p.out_parent[slot] = node;
     p.out_ray[slot] = ray;
+    if (p.out_adv) p.out_adv[slot] = p.restart ? adv : adv + e.t;
   }
   warp_set_bit(p.fault_bits, faulted && fault_block < p.fault_bit_limit ? fault_block : -1);
   warp_set_bit(p.hit_bits, hit ? 2 * (node / p.nodes_in_block) + dup : -1);
@@ -627,10 +646,11 @@ __global__ void __launch_bounds__(kBlockThreads) trace_kernel(const __grid_const
   if (r >= total) return;
   uint32_t ray;
   float4 o, d;
-  if (!ray_at<kFirst>(p, r, ray, o, d)) return;
+  float adv;
+  if (!ray_at<kFirst>(p, r, ray, o, d, adv)) return;
   uint32_t fetches = 0, far_fetches = 0;
   const RayEnd e = cast_ray<kCount>(p, o, d, fetches, far_fetches);
-  end_ray<kCount>(p, e, ray, o, d, fetches, far_fetches);
+  end_ray<kCount>(p, e, ray, o, d, adv, fetches, far_fetches);
 }
 
 // Persistent form: one CTA per SM slot; every warp takes rays from the
@@ -647,6 +667,7 @@ __global__ void __launch_bounds__(kBlockThreads) trace_persistent_kernel(const _
   Cast c;
   int outcome = kRunning;
   uint32_t ray = 0;
+  float adv = 0.0f;
   bool have = false, exhausted = false;
   uint32_t fetches = 0, far_fetches = 0;
 
@@ -662,7 +683,7 @@ __global__ void __launch_bounds__(kBlockThreads) trace_persistent_kernel(const _
       if (!have) {
         const int r = base + __popc(idle & ((1u << lane) - 1));
         float4 o, d;
-        if (r < total && ray_at<kFirst>(p, r, ray, o, d)) {
+        if (r < total && ray_at<kFirst>(p, r, ray, o, d, adv)) {
           s_origin[threadIdx.x] = o;  // kept for the ray's fault record
           s_dir[threadIdx.x] = d;
           cast_begin(c, p.root, o, d);
@@ -687,7 +708,7 @@ __global__ void __launch_bounds__(kBlockThreads) trace_persistent_kernel(const _
       e.dup = (int)((c.desc >> 9) & 1u);
       e.error = outcome == kError;
       e.iter = c.iter;
-      end_ray<kCount>(p, e, ray, s_origin[threadIdx.x], s_dir[threadIdx.x], fetches, far_fetches);
+      end_ray<kCount>(p, e, ray, s_origin[threadIdx.x], s_dir[threadIdx.x], adv, fetches, far_fetches);
       have = false;
       outcome = kRunning;
     }
@@ -710,28 +731,32 @@ __global__ void __launch_bounds__(kBlockThreads) trace_queue_kernel(const __grid
     const int r = base + lane;
     uint32_t ray;
     float4 o, d;
-    if (r < total && ray_at<kFirst>(p, r, ray, o, d)) {
+    float adv;
+    if (r < total && ray_at<kFirst>(p, r, ray, o, d, adv)) {
       if (!kFirst && p.finish_mask && ((p.finish_mask >> slot_of(p, ray)) & 1ull)) {
         // served mode: the request stops here; FinishTracingFrame's shading
         // with the fault's parent node
         const uchar4 col = (p.normals && p.colors) ? shade(p, p.in_parent[r]) : make_uchar4(0, 0, 0, 0);
         p.image[ray] = finish(p, col);
+        if (p.depth) write_depth(p, ray, adv, p.in_parent[r]);
       } else {
         uint32_t fetches = 0, far_fetches = 0;
         const RayEnd e = cast_ray<kCount>(p, o, d, fetches, far_fetches);
-        end_ray<kCount>(p, e, ray, o, d, fetches, far_fetches);
+        end_ray<kCount>(p, e, ray, o, d, adv, fetches, far_fetches);
       }
     }
   }
 }
 
 // FinishTracingFrame for rays still faulted at the end of the frame: shade
-// with the fault's parent node as the cache holds it now.
+// with the fault's parent node as the cache holds it now.  Depth output: the
+// distance at which the ray stopped and that parent node.
 __global__ void __launch_bounds__(kBlockThreads) finish_kernel(const __grid_constant__ TraceParams p) {
   const int i = blockIdx.x * kBlockThreads + threadIdx.x;
   if (i >= *p.n_in) return;
   const uchar4 col = (p.normals && p.colors) ? shade(p, p.in_parent[i]) : make_uchar4(0, 0, 0, 0);
   p.image[p.in_ray[i]] = finish(p, col);
+  if (p.depth) write_depth(p, p.in_ray[i], p.in_adv[i], p.in_parent[i]);
 }
 
 // raytracer.cl:18-71 (RaytraceKernel, the reference's debug depth view) for

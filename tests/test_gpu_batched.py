@@ -161,3 +161,26 @@ def test_graphs_match_plain_launches(trees):
         assert a[0] == b[0], "frame %d" % f
         for v in range(len(sizes)):
             np.testing.assert_array_equal(a[1][v], b[1][v], err_msg="frame %d view %d" % (f, v))
+
+
+def test_batched_depth_output_vs_oracle(trees):
+    """Streamed batched frames with depth output on: every view's depth bits
+    and hit nodes equal the oracle's batched frame."""
+    from oracle import oracle as O
+    frames = [[_matrix(c, w, h) for c, (w, h) in zip(_cams(len(SIZES), 25.0 * f), SIZES)] for f in range(4)]
+    libc_srand(23)
+    sc = O.OracleScene(trees["terrain8s"], 250, views=SIZES)
+    ld, cm, rt = _gpu_views(trees["terrain8s"], 250, SIZES, seed=23)
+    rt.set_depth_output(True)
+    for f, mats in enumerate(frames):
+        n, imgs = sc.render_views(mats)
+        ref = sc.depth()
+        rt.RenderViews(mats)
+        assert rt.stats()["passes"] == n, "frame %d" % f
+        for v in range(len(SIZES)):
+            d, nodes = rt.read_depth(view=v)
+            np.testing.assert_array_equal(nodes, ref[v][1], err_msg="frame %d view %d" % (f, v))
+            np.testing.assert_array_equal(d.view(np.uint32), ref[v][0].view(np.uint32),
+                                          err_msg="frame %d view %d" % (f, v))
+            np.testing.assert_array_equal(rt.read_image(view=v), imgs[v], err_msg="frame %d view %d" % (f, v))
+    sc.close()

@@ -190,3 +190,62 @@ def test_lod_pressure_policy(trees):
     for (l0, f0), (l1, _) in zip(on, on[1:]):  # grows after a filled session, never beyond the cap (float math)
         assert f32(l1) == (min(f32(32.0), f32(l0) * f32(2.0)) if f0 else max(f32(1.0), f32(l0) / f32(1.25)))
     assert any(f == 0 for _, f in on)  # a coarser frame fits in the cache
+
+
+def _bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+@pytest.mark.parametrize("name,max_passes", [("stream8", 0), ("stream8_lod0", 0), ("c1_stream", 0), ("stream8", 2)])
+def test_depth_output_vs_oracle(trees, name, max_passes):
+    """Depth and hit-node buffers of streamed frames equal the oracle's bit for
+    bit (depth compared as float bits: a faulted ray's advances add up in the
+    same order), including rays a pass cap leaves faulted, which end with the
+    distance where they stopped and their fault's parent node."""
+    from oracle import oracle as O
+    case = FRAME_CASES[name]
+    w, h = case["size"]
+    mats = [_matrix(c, w, h) for c in case["cameras"]]
+    libc_srand(case["seed"])
+    sc = O.OracleScene(trees[case["tree"]], case["max_blocks"], w, h, case["lod"], max_passes=max_passes)
+    ld, cm, rt = _scene(trees[case["tree"]], case["max_blocks"], w, h, case["lod"], case["seed"])
+    rt.set_max_passes(max_passes)
+    rt.set_depth_output(True)
+    capped = 0
+    for i, m in enumerate(mats):
+        passes, ref = sc.render(m)
+        dref, nref = sc.depth()
+        rt.RenderFrame(m)
+        st = rt.stats()
+        assert st["passes"] == passes, i
+        capped += int(max_passes > 0 and passes == max_passes and st["faults"] > 0)
+        np.testing.assert_array_equal(rt.read_image(), ref, err_msg="frame %d" % i)
+        d, n = rt.read_depth()
+        np.testing.assert_array_equal(n, nref, err_msg="frame %d hit nodes" % i)
+        np.testing.assert_array_equal(_bits(d), _bits(dref), err_msg="frame %d depth" % i)
+    assert np.isposinf(dref).any() and np.isfinite(dref).any()
+    if max_passes:
+        assert capped > 0  # some frame ended at the cap with rays still faulted
+    sc.close()
+
+
+def test_depth_output_resident_full_hd(trees):
+    """1920x1080 on the resident depth-10 scene: depth bits and hit nodes equal
+    the oracle's on every pixel; turning the output off leaves the image alone."""
+    from oracle import oracle as O
+    w, h = 1920, 1080
+    m = _matrix(C1_CAMERA, w, h)
+    sc = O.OracleScene(trees["terrain10"], 0, w, h, 1.0)
+    _, ref = sc.render(m)
+    dref, nref = sc.depth()
+    sc.close()
+    ld, cm, rt = _scene(trees["terrain10"], 0, w, h)
+    rt.set_depth_output(True)
+    rt.RenderFrame(m)
+    d, n = rt.read_depth()
+    np.testing.assert_array_equal(n, nref)
+    np.testing.assert_array_equal(_bits(d), _bits(dref))
+    np.testing.assert_array_equal(rt.read_image(), ref)
+    rt.set_depth_output(False)
+    rt.RenderFrame(m)
+    np.testing.assert_array_equal(rt.read_image(), ref)
