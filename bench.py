@@ -77,6 +77,9 @@ def parse():
     ap.add_argument("--cache-mib", type=int, default=None, help="override the workload's cache size")
     ap.add_argument("--depth", type=int, default=None, help="override the workload's octree depth")
     ap.add_argument("--c2-log2n", type=int, default=28, help="c2: 2^k feedback words (profiling uses a smaller k)")
+    ap.add_argument("--parity-frames", type=int, default=5,
+                    help="frame workloads: after timing, compare this many timed frames (and the warm-up frames "
+                         "before them) with the oracle, untimed; 0 skips the check")
     a = ap.parse_args()
     if a.workload in WORKLOADS:
         if a.spheres is not None:
@@ -206,17 +209,41 @@ class roofline_range:
         torch.cuda.nvtx.range_pop()
 
 
+def profile_values(name):
+    """'key: number' lines of the committed ncu summary profiles/<name>.md."""
+    out = {}
+    try:
+        for line in open(os.path.join(ROOT, "profiles", name + ".md")):
+            k, sep, v = line.partition(":")
+            if sep and k.strip() in ("traffic_bytes_per_launch", "alg_bytes_per_launch"):
+                try:
+                    out[k.strip()] = float(v)
+                except ValueError:
+                    pass
+    except OSError:
+        pass
+    return out
+
+
 def profile_traffic(name):
     """DRAM bytes per launch of the traversal kernel from the committed ncu
     summary (profiles/<name>.md, line 'traffic_bytes_per_launch: N')."""
-    p = os.path.join(ROOT, "profiles", name + ".md")
-    try:
-        for line in open(p):
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":")[1])
-    except OSError:
-        pass
-    return None
+    return profile_values(name).get("traffic_bytes_per_launch")
+
+
+def scaled_traffic(name, alg_bytes):
+    """DRAM bytes of the timed launch: the profiled launch's DRAM bytes
+    (profiles/<name>.md) scaled by the ratio of the two launches' algorithmic
+    bytes, when the profile records its own ('alg_bytes_per_launch: N'); the
+    factor is 1 when the profile captured the same camera.  Returns (bytes,
+    rule)."""
+    v = profile_values(name)
+    t, a = v.get("traffic_bytes_per_launch"), v.get("alg_bytes_per_launch")
+    if t is None:
+        return None, "no profile"
+    if not a:
+        return t, "profiled launch as is"
+    return round(t * alg_bytes / a), "profiled DRAM bytes x (algorithmic bytes of this launch / of the profiled launch)"
 
 
 # ---------------------------------------------------------------------------
@@ -280,14 +307,86 @@ def cache_blocks(cfg):
 
 
 # ---------------------------------------------------------------------------
-def run_cpu_frames(path, cfg, mats, budget_s):
+def frames_parity(path, cfg, mats, seed=1, timed=None, timed_first=0):
+    """Untimed parity check of the per-frame path on the workload itself: the
+    oracle and a fresh GPU cache + renderer (feedback words recorded, depth
+    output on) render the same frames from the same initial fill with the same
+    hit-window seed, and every frame's pass count, every pass's per-pixel
+    feedback words, image, depth bits and hit nodes are compared, then the
+    cache buffers after the last frame.  `timed` holds images the timed run
+    produced for frames timed_first, timed_first + 1, ...; they are compared
+    with the oracle's frames too."""
+    import ctypes
+
+    import rayt_gb300 as R
+    from oracle import oracle as O
+    w, h = cfg["width"], cfg["height"]
+    blocks = cache_blocks(cfg)
+    t0 = time.time()
+    ld = R.StoredOctreeLoader(path)
+    cm = R.GPUOctreeCacheManager(blocks, ld)
+    cm.InitialFillCache()
+    rt = R.GPURayTracer(cm, w, h)
+    rt.set_lod_voxel_size(cfg["lod"])
+    rt.set_frame_time_limit(1e30)
+    rt.seed(seed)
+    rt.record_passes(True)
+    rt.set_depth_output(True)
+    sc = O.OracleScene(path, blocks, w, h, cfg["lod"], 1e30)
+    sc.record(True)
+    ctypes.CDLL(None).srand(ctypes.c_uint(seed))
+    out = {"frames": 0, "pixels_differing": 0, "passes_equal": True, "pass_words_equal": True,
+           "depth_bits_equal": True, "hit_nodes_differing": 0, "timed_frames_checked": 0,
+           "timed_pixels_differing": 0, "passes": 0, "uploaded_blocks": 0}
+    for i, m in enumerate(mats):
+        n, img = sc.render(m)
+        dref, nref = sc.depth()
+        rt.RenderFrame(m)
+        st = rt.stats()
+        out["frames"] += 1
+        out["passes"] += n
+        out["uploaded_blocks"] += st["uploaded_blocks"]
+        out["passes_equal"] &= st["passes"] == n
+        out["pixels_differing"] += int((rt.read_image() != img).any(axis=2).sum())
+        for p in range(min(n, st["passes"])):
+            out["pass_words_equal"] &= bool(np.array_equal(rt.pass_words(p), sc.pass_words(p)))
+        d, nodes = rt.read_depth()
+        out["depth_bits_equal"] &= bool(np.array_equal(d.view(np.uint32), dref.view(np.uint32)))
+        out["hit_nodes_differing"] += int((nodes != nref).sum())
+        k = i - timed_first
+        if timed is not None and 0 <= k < len(timed):
+            out["timed_frames_checked"] += 1
+            out["timed_pixels_differing"] += int((timed[k] != img).any(axis=2).sum())
+    nodes = sc.max_blocks * sc.nib
+    same = True
+    for ch, name in enumerate(["node links", "normals", "colors"]):
+        same &= bool(np.array_equal(cm.read_buffer(name), sc.read(ch, nodes * 4)))
+    same &= bool(np.array_equal(cm.read_buffer("far pointers"), sc.read(-1, sc.max_blocks * 32)))
+    out["cache_buffers_equal"] = same
+    out["seconds"] = round(time.time() - t0, 1)
+    sc.close()
+    del rt, cm, ld
+    out["ok"] = bool(out["passes_equal"] and out["pass_words_equal"] and out["depth_bits_equal"] and same
+                     and out["pixels_differing"] == 0 and out["hit_nodes_differing"] == 0
+                     and out["timed_pixels_differing"] == 0)
+    return out
+
+
+def run_cpu_frames(path, cfg, mats, budget_s, warm=()):
     """The oracle (reference algorithm on host cores) over the same frames, until
-    the frames run out or the time budget is spent.  Returns (rays, seconds,
-    frames, setup_seconds)."""
+    the frames run out or the time budget is spent, after rendering the
+    warm-up frames `warm` untimed (the cache then holds what the GPU arm's
+    cache held when its timing began).  Returns (rays, seconds, frames,
+    setup_seconds)."""
+    import ctypes
+
     from oracle import oracle as O
     w, h = cfg["width"], cfg["height"]
     t0 = time.time()
     sc = O.OracleScene(path, cache_blocks(cfg), w, h, cfg["lod"], 1e30)
+    ctypes.CDLL(None).srand(ctypes.c_uint(1))
+    for m in warm:
+        sc.render(m)
     setup = time.time() - t0
     rays, el, n = 0, 0.0, 0
     for m in mats:
@@ -317,11 +416,13 @@ def bench_frames(args, rank, world, local):
     if args.impl == "reference":
         if rank != 0:
             return None
-        rays, el, n, setup = run_cpu_frames(path, cfg, mats[args.warmup:], args.cpu_seconds * 3)
+        rays, el, n, setup = run_cpu_frames(path, cfg, mats[args.warmup:], args.cpu_seconds * 3,
+                                            warm=mats[:args.warmup])
         v = rays / el / 1e6
-        sample = "%d of %d frames at %dx%d (oracle, OpenMP)" % (n, steps, w, h)
+        sample = ("%d of %d frames at %dx%d after the same %d warm-up frames (oracle, OpenMP)"
+                  % (n, steps, w, h, args.warmup))
         return {"metric": "Mrays/s at %dx%d (frames of the per-frame path)" % (w, h), "value": round(v, 3),
-                "unit": "Mrays/s", "impl": "reference", "n_gpus": 1, "steps": n, "warmup": 0,
+                "unit": "Mrays/s", "impl": "reference", "n_gpus": 1, "steps": n, "warmup": args.warmup,
                 "ms_per_step": round(el / n * 1e3, 3), "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": wl, "width": w, "height": h, "depth": cfg["depth"],
@@ -339,10 +440,11 @@ def bench_frames(args, rank, world, local):
     rt = R.GPURayTracer(cm, w, h)
     rt.set_lod_voxel_size(cfg["lod"])
     rt.set_frame_time_limit(1e30)
+    rt.seed(1)  # the hit-window generator; the parity check replays the same sequence
     stream = torch.cuda.ExternalStream(rt.stream_handle())
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > L2 (129 MB)
-    img = np.zeros((h, w, 4), np.uint8)
     pinned = torch.empty((h, w, 4), dtype=torch.uint8).pin_memory()
+    timed_imgs = []  # the first parity_frames timed images, checked against the oracle afterwards
 
     for i in range(args.warmup):
         rt.RenderFrame(mats[i])
@@ -366,6 +468,8 @@ def bench_frames(args, rank, world, local):
         # end to end: the frame's RGBA8 image read back to pinned host memory
         R._check(R.lib().rayt_renderer_read_image(rt._h, pinned.data_ptr(), pinned.numel()))
         wall += time.perf_counter() - t
+        if len(timed_imgs) < args.parity_frames:
+            timed_imgs.append(pinned.numpy().copy())
         e1.synchronize()
         d = e0.elapsed_time(e1)
         ms_dev += d
@@ -395,13 +499,18 @@ def bench_frames(args, rank, world, local):
     alg_bytes = 4 * fetch["link_fetches"] + 4 * fetch["far_fetches"] + 16 * fetch["rays"]
     achieved = alg_bytes / (pass_ms / 1e3) / 1e9
     peak, peak_kind = hbm_peak()
-    traffic = profile_traffic("trace_kernel_%s" % wl)
+    traffic, traffic_rule = scaled_traffic("trace_kernel_%s" % wl, alg_bytes)
 
     cpu = None
     if rank == 0:
-        crays, cel, cn, _ = run_cpu_frames(path, cfg, mats[args.warmup:], args.cpu_seconds)
+        crays, cel, cn, _ = run_cpu_frames(path, cfg, mats[args.warmup:], args.cpu_seconds, warm=mats[:args.warmup])
         cpu = {"value": round(crays / cel / 1e6, 3), "unit": "Mrays/s", "cores": os.cpu_count() or 1, "kind": "port",
-               "sample": "%d frames at %dx%d of the same workload (oracle, OpenMP)" % (cn, w, h)}
+               "sample": "%d frames at %dx%d of the same workload after the same %d warm-up frames (oracle, OpenMP)"
+                         % (cn, w, h, args.warmup)}
+    parity = None
+    if rank == 0 and args.parity_frames > 0:
+        parity = frames_parity(path, cfg, mats[:args.warmup + args.parity_frames], seed=1, timed=timed_imgs,
+                               timed_first=args.warmup)
     if rank != 0:
         return None
     lat_sorted = np.sort(np.array(lat))
@@ -422,11 +531,14 @@ def bench_frames(args, rank, world, local):
                    "trace_ms_per_frame": round(trace_ms / steps, 4),
                    **{k.replace("_ms_", "_") + "_ms_per_frame": round(v / steps, 4) for k, v in part_ms.items()}},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
+                     "frac": round(achieved / peak, 4), "traffic": traffic, "traffic_rule": traffic_rule,
+                     "peak_source": peak_kind,
                      "kernel": "trace_kernel<first pass>", "launch_ms": round(pass_ms, 4),
-                     "bytes_per_ray": round(alg_bytes / fetch["rays"], 2),
-                     "link_fetches_per_ray": round(fetch["link_fetches"] / fetch["rays"], 3)},
+                     "alg_bytes": int(alg_bytes), "bytes_per_ray": round(alg_bytes / fetch["rays"], 2),
+                     "link_fetches_per_ray": round(fetch["link_fetches"] / fetch["rays"], 3),
+                     "iterations_per_ray": round(fetch["iterations"] / fetch["rays"], 3)},
         "cpu_baseline": cpu,
+        "parity": parity,
         "gpu_launches": int(launches),
         "clocks": clk,
     }
