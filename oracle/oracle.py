@@ -137,6 +137,23 @@ class OracleScene:
             o += w * h
         return out
 
+    def render_size(self, w, h, mat, lod=1.0):
+        """A one-view frame of size (w, h) over this scene's cache, by a second
+        renderer kept per size (for a resident cache: the frame any renderer
+        would draw).  Returns (passes, image)."""
+        if not hasattr(self, "_extra"):
+            self._extra = {}
+        if (w, h) not in self._extra:
+            self._extra[w, h] = lib().oracle_renderer_create(self.cache, w, h, lod, 1e30, 0)
+        r = self._extra[w, h]
+        m, p = _m(mat)
+        n = lib().oracle_render_frame(r, p)
+        if n < 0:
+            raise RuntimeError("oracle: " + lib().oracle_last_error().decode())
+        img = np.zeros((h, w, 4), np.uint8)
+        lib().oracle_frame_image(r, img.ctypes.data)
+        return n, img
+
     def trace_once(self, mat):
         m, p = _m(mat)
         words = np.zeros(self.w * self.h, np.int32)
@@ -164,6 +181,9 @@ class OracleScene:
 
     def close(self):
         L = lib()
+        for r in getattr(self, "_extra", {}).values():
+            L.oracle_renderer_destroy(r)
+        self._extra = {}
         if self.r:
             L.oracle_renderer_destroy(self.r)
             self.r = None
