@@ -155,6 +155,9 @@ typedef struct {
   int64_t bytes_h2d;         /* host->device bytes for block uploads */
   int64_t bytes_read;        /* bytes read from the block file */
   double io_seconds;         /* host time spent reading the file */
+  double io_wait_seconds;    /* host time a transaction waited for its block reads */
+  double place_seconds;      /* host time placing blocks (slot choice, links, patches) */
+  double flush_seconds;      /* host time submitting copies and upload kernels */
 } rayt_cache_stats;
 int rayt_cache_stats_get(const rayt_cache* cache, rayt_cache_stats* out);
 

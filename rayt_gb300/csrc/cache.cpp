@@ -646,13 +646,18 @@ int Cache::EndTransaction() {
     StartRead(pending_.data() + i, n);
     i += n;
   };
+  using clock = std::chrono::steady_clock;
+  auto secs = [](clock::time_point a) { return std::chrono::duration<double>(clock::now() - a).count(); };
   if (!pending_.empty() && staged_ == stage_cap_) rc = NextHalf();
   if (rc == RAYT_OK && !TransactionFilled()) start_chunk();
   while (rc == RAYT_OK && chunk_first >= 0) {
+    auto t = clock::now();
     FinishRead();
+    stats_.io_wait_seconds += secs(t);
     const int first = chunk_first, n = chunk_n;
     chunk_first = -1;
     if (!filled && !TransactionFilled()) start_chunk();  // read ahead while placing
+    t = clock::now();
     for (int k = 0; k < n && !filled; ++k) {
       if (TransactionFilled()) {
         filled = true;
@@ -661,6 +666,7 @@ int Cache::EndTransaction() {
       if (block_slot_[meta_[(size_t)stage_cap_ * half_ + first + k].block] >= 0) continue;
       if ((rc = Place(first + k, nullptr)) != RAYT_OK) break;
     }
+    stats_.place_seconds += secs(t);
     if (rc != RAYT_OK || filled) break;
     if (chunk_first < 0 && i < pending_.size()) {  // the half is full: continue in the other one
       if ((rc = NextHalf()) != RAYT_OK) break;
@@ -669,7 +675,9 @@ int Cache::EndTransaction() {
   }
   if (chunk_first >= 0) FinishRead();  // a read-ahead the transaction no longer needs
   pending_.clear();
+  const auto tf = clock::now();
   const int frc = FlushTo(staged_);
+  stats_.flush_seconds += secs(tf);
   in_transaction_ = false;
   DropMarker(kTransaction);
   return rc != RAYT_OK ? rc : frc;
