@@ -19,6 +19,7 @@
 // kernel - instead of per-channel and per-pointer clEnqueueWriteBuffer calls.
 #include "cache.h"
 
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
@@ -29,6 +30,65 @@
 #include <thread>
 
 namespace rayt {
+
+// The distinct child blocks named by one block's fault links: an open-
+// addressing set cleared in O(1) by a generation stamp, growing with the
+// count (a block usually names a few dozen children, so the table stays in
+// L1).  One per reading thread.
+class ChildSet {
+ public:
+  void Clear() {
+    n_ = 0;
+    last_ = UINT32_MAX;
+    if (++gen_ == 0) {  // stamps wrapped: forget every slot
+      std::fill(stamp_.begin(), stamp_.end(), 0u);
+      gen_ = 1;
+    }
+  }
+  // True when v was not in the set (and is now).
+  bool Insert(uint32_t v) {
+    if (v == last_) return false;  // repeats are mostly adjacent links
+    last_ = v;
+    if (2 * (n_ + 1) > stamp_.size()) Grow();
+    const uint32_t mask = (uint32_t)stamp_.size() - 1;
+    for (uint32_t h = (v * 2654435761u) & mask;; h = (h + 1) & mask) {
+      if (stamp_[h] != gen_) {
+        stamp_[h] = gen_;
+        key_[h] = v;
+        ++n_;
+        return true;
+      }
+      if (key_[h] == v) return false;
+    }
+  }
+
+ private:
+  std::vector<uint32_t> key_, stamp_;
+  uint32_t gen_ = 1, n_ = 0, last_ = UINT32_MAX;
+  void Grow() {
+    const size_t size = stamp_.empty() ? 1024 : stamp_.size() * 4;
+    std::vector<uint32_t> keys;
+    for (size_t i = 0; i < stamp_.size(); ++i)
+      if (stamp_[i] == gen_) keys.push_back(key_[i]);
+    key_.assign(size, 0u);
+    stamp_.assign(size, 0u);
+    gen_ = 1;
+    const uint32_t mask = (uint32_t)size - 1;
+    for (uint32_t v : keys) {
+      uint32_t h = (v * 2654435761u) & mask;
+      while (stamp_[h] == gen_) h = (h + 1) & mask;
+      stamp_[h] = gen_;
+      key_[h] = v;
+    }
+  }
+};
+
+namespace {
+ChildSet& child_set() {
+  thread_local ChildSet s;
+  return s;
+}
+}  // namespace
 
 // Threads that read staged blocks from the file in parallel.  Run() returns
 // only after every item is done and every worker has left the job, so the
@@ -438,9 +498,14 @@ int Cache::ReadOne(int pos, int block) {
     }
   }
   const uint32_t* links = reinterpret_cast<const uint32_t*>(area + 80);
+  // Fault links name child blocks, most of them many times: keep each child
+  // once, in order of first appearance (Place records a child under the first
+  // link that names it, so later repeats change nothing there).
+  ChildSet& seen = child_set();
+  seen.Clear();
   if (validated_[block]) {  // links checked on an earlier load: only the fault children
     for (int n = 0; n < nib_; ++n)
-      if ((links[n] & 255u) && ((links[n] >> 8) & 1u)) m.faults.push_back(links[n] >> 11);
+      if ((links[n] & 255u) && ((links[n] >> 8) & 1u) && seen.Insert(links[n] >> 11)) m.faults.push_back(links[n] >> 11);
     return RAYT_OK;
   }
   for (int n = 0; n < nib_; ++n) {
@@ -453,7 +518,7 @@ int Cache::ReadOne(int pos, int block) {
       continue;
     }
     if (ptr >= blocks) return bad("fault link points past the last block");
-    m.faults.push_back(ptr);
+    if (seen.Insert(ptr)) m.faults.push_back(ptr);
   }
   validated_[block] = 1;  // one byte per block: threads reading other blocks touch other bytes
   return RAYT_OK;
