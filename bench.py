@@ -1,6 +1,7 @@
 """Benchmark of the per-frame path on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload c3|c1|c2|c4|c5]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload c3|c1|c2|c2r|c4|c5|c5p]
 
 The default workload is c3, the configuration the Mrays/s-at-1080p metric is
 quoted on.
@@ -15,14 +16,17 @@ builder; no public dataset is involved):
       a seeded Catmull-Rom spline, block cache capped at 2 GiB, blocks
       streamed from the file
   c2  2^28 feedback words: 90% NO_HIT, Zipf(1.1) block IDs over 2^24
+  c2r the same with block IDs over 2^28: the kept keys span more than 2^26
+      values, so unique runs the LSD radix passes instead of the bitmap
   c4  the c3 scene, 64 views per frame of sizes drawn from {256^2, 640x480,
       1280x720, 1920x1080} (seed 7), view v on its own spline (seed 7 + v),
       through the batched renderer; the plain per-view path is timed beside it
-  c5  depth-14 heightfield + spheres (16384^3), 16 clients of sizes drawn from
-      {1280x720, 1920x1080, 2560x1440} (seed 100), client c on its own spline
-      (seed 100 + c), frame requests Poisson at 60 Hz per client (seed 11),
-      through the server (continuous batching, 40 GB shared cache) and through
-      the plain per-frame path on the same schedule
+  c5  depth-14 heightfield + spheres (16384^3, 16384-node blocks), 16 clients
+      of sizes drawn from {1280x720, 1920x1080, 2560x1440} (seed 100), client
+      c on its own spline (seed 100 + c), frame requests Poisson at 60 Hz per
+      client (seed 11), through the server (continuous batching, 40 GiB shared
+      cache) and through the plain per-frame path on the same schedule
+  c5p c5 with a 6 GiB shared cache, below the tree: shared-LRU eviction
 
 --impl reference times the reference algorithm's CPU implementation (the
 oracle restatement in oracle/, all host threads) on the same workload.
@@ -54,15 +58,19 @@ WORKLOADS = {
     # frame measures batched traversal + feedback rather than streaming
     "c4": {"depth": 12, "spheres": 2000, "width": 0, "height": 0, "cache_bytes": 0, "lod": 1.0, "views": 64,
            "sizes": [(256, 256), (640, 480), (1280, 720), (1920, 1080)], "size_seed": 7},
-    # 16 clients, Poisson 60 Hz each, against one shared cache of up to 40 GB.
-    # The cache format's 21-bit far-pointer slots address fewer than 2^18
-    # blocks, so the scene uses 8192-node blocks: the cache then holds up to
-    # 25.8 GB, which is more than the whole tree (about 16 GB)
-    "c5": {"depth": 14, "spheres": 2000, "width": 0, "height": 0, "cache_bytes": 40 << 30, "nib": 8192,
+    # 16 clients, Poisson 60 Hz each, against one shared 40 GiB cache.  The
+    # cache format's 21-bit far-pointer slots address fewer than 2^18 blocks,
+    # so the scene uses 16384-node blocks: 40 GiB is 218453 of them (3.6 G
+    # nodes, node indices unsigned 32-bit), more than the whole tree
+    "c5": {"depth": 14, "spheres": 2000, "width": 0, "height": 0, "cache_bytes": 40 << 30, "nib": 16384,
            "lod": 1.0,
            "clients": 16, "sizes": [(1280, 720), (1920, 1080), (2560, 1440)], "size_seed": 100,
            "rate_hz": 60.0, "arrival_seed": 11, "seconds": 2.0, "closed_frames": 20, "max_passes": 8},
 }
+# The served workload under cache pressure: the same scene and clients with a
+# 6 GiB cache, well below the tree, so the clients' blocks evict one another
+# from the shared LRU
+WORKLOADS["c5p"] = dict(WORKLOADS["c5"], cache_bytes=6 << 30)
 
 
 def parse():
@@ -71,7 +79,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=0)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4", "c5"])
+    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c2r", "c3", "c4", "c5", "c5p"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU baseline sample")
     ap.add_argument("--spheres", type=int, default=None, help="override the workload's sphere count")
     ap.add_argument("--cache-mib", type=int, default=None, help="override the workload's cache size")
@@ -741,7 +749,7 @@ def bench_served(args, rank, world, local):
     import torch
 
     import rayt_gb300 as R
-    wl = "c5"
+    wl = args.workload
     cfg = WORKLOADS[wl]
     closed_frames = args.steps or cfg["closed_frames"]
     path = scene_path(wl, local, world)
@@ -751,7 +759,8 @@ def bench_served(args, rank, world, local):
     nframes = max(frames_per_client + [closed_frames + args.warmup]) + 1
     cams = [camera_path("c3", nframes, w, h, seed=cfg["size_seed"] + c) for c, (w, h) in enumerate(sizes)]
     pixels = [w * h for w, h in sizes]
-    metric = "frames/s at 16 clients (served, continuous batching), depth 14"
+    metric = "frames/s at 16 clients (served, continuous batching), depth 14" + (
+        ", %d GiB cache (evicting)" % (cfg["cache_bytes"] >> 30) if wl == "c5p" else "")
     threads = os.cpu_count() or 1
     t_begin = time.time()
 
@@ -944,6 +953,10 @@ def bench_served(args, rank, world, local):
                 "d2h_bytes_per_step": int(mean_px * 4)},
         "served": {"closed_loop_frames_s": round(value, 2),
                    "closed_loop_mrays_s": round(n_served * mean_px / el_served / 1e6, 1),
+                   "closed_loop_ticks": int(st["ticks"]),
+                   "closed_loop_uploaded_blocks": int(st["uploaded_blocks"]),
+                   "host_ms_per_tick": {k: round(st["host_ms_" + k] / max(1, st["ticks"]), 4)
+                                        for k in ("wait", "lru", "load")},
                    "open_loop": {"offered_frames_s": round(len(sched) / cfg["seconds"], 1),
                                  "frames_s": round(len(infos) / span_served, 1), "p50_ms": sp50, "p99_ms": sp99,
                                  "passes_mean": round(float(np.mean([i["passes"] for i in infos])), 3),
@@ -1028,7 +1041,10 @@ def bench_c2(args, rank, world, local):
     import rayt_gb300 as R
     n = 1 << args.c2_log2n
     steps = args.steps or 20
-    words = zipf_words(n)
+    wl = args.workload
+    # c2r: block IDs over 2^28 instead of 2^24, so the kept keys span more than
+    # 2^26 values and unique takes the LSD radix passes instead of the bitmap
+    words = zipf_words(n, blocks=(1 << 28) if wl == "c2r" else (1 << 24))
     if args.impl == "reference":
         if rank != 0:
             return None
@@ -1041,11 +1057,11 @@ def bench_c2(args, rank, world, local):
             k += 1
         el = (time.time() - t) / k
         v = sub.size / el / 1e9
-        return {"metric": "Gkeys/s feedback compaction+sort+unique (2^%d words)" % args.c2_log2n, "value": round(v, 4),
+        return {"metric": "Gkeys/s feedback compaction+sort+unique (2^%d words%s)" % (args.c2_log2n, ", radix path" if wl == "c2r" else ""), "value": round(v, 4),
                 "unit": "Gkeys/s", "impl": "reference", "n_gpus": 1, "steps": k, "warmup": 0,
                 "ms_per_step": round(el * 1e3, 3), "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-                "config": {"workload": "c2", "n": n, "sample_n": sub.size},
+                "config": {"workload": wl, "n": n, "sample_n": sub.size},
                 "cpu_baseline": {"value": round(v, 4), "unit": "Gkeys/s", "cores": os.cpu_count() or 1, "kind": "port",
                                  "sample": "2^22 of the 2^28 words per step (merge sort + Hillis-Steele scan)"},
                 "e2e": {"value": round(v, 4), "unit": "Gkeys/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -1097,11 +1113,12 @@ def bench_c2(args, rank, world, local):
         k += 1
     cpu = {"value": round(sub.size * k / (time.time() - t) / 1e9, 4), "unit": "Gkeys/s", "cores": os.cpu_count() or 1,
            "kind": "port", "sample": "%d calls on 2^22 of the words (merge sort + Hillis-Steele scan)" % k}
-    return {"metric": "Gkeys/s feedback compaction+sort+unique (2^%d words)" % args.c2_log2n,
+    return {"metric": "Gkeys/s feedback compaction+sort+unique (2^%d words%s)" % (args.c2_log2n, ", radix path" if wl == "c2r" else ""),
             "value": round(sum_over_ranks(n * steps, world) / t_dev / 1e9, 4), "unit": "Gkeys/s", "n_gpus": world,
             "steps": steps, "warmup": args.warmup, "ms_per_step": round(t_dev / steps * 1e3, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": {"workload": "c2", "n": n, "kept": m, "unique": cnt,
+            "config": {"workload": wl, "n": n, "kept": m, "unique": cnt, "key_span": span,
+                       "block_ids": (1 << 28) if wl == "c2r" else (1 << 24),
                        "l2": "inputs (%d MiB) larger than L2" % (4 * n >> 20) if 4 * n > (129 << 20) else "inputs in L2"},
             "e2e": {"value": round(n * steps / t_e2e / 1e9, 4), "unit": "Gkeys/s", "h2d_bytes_per_step": 4 * n,
                     "d2h_bytes_per_step": 4 * cnt},
@@ -1122,11 +1139,11 @@ def main():
         rank, world, local = 0, 1, 0
     else:
         rank, world, local = dist_setup(args.gpus)
-    if args.workload == "c2":
+    if args.workload in ("c2", "c2r"):
         out = bench_c2(args, rank, world, local)
     elif args.workload == "c4":
         out = bench_batched(args, rank, world, local)
-    elif args.workload == "c5":
+    elif args.workload in ("c5", "c5p"):
         out = bench_served(args, rank, world, local)
     else:
         out = bench_frames(args, rank, world, local)

@@ -333,6 +333,10 @@ typedef struct {
 } rayt_request_info;
 typedef struct {
   int64_t submitted, completed, ticks, rays_traced, faults, kernel_launches, bytes_d2h;
+  int64_t uploaded_blocks;   /* blocks streamed into the shared cache by ticks */
+  double host_ms_wait;       /* host time blocked on the GPU (tick passes), summed over ticks */
+  double host_ms_lru;        /* feedback decode, LRU marks and block requests */
+  double host_ms_load;       /* EndTransaction: block reads, placement (evictions), upload issue */
 } rayt_server_stats;
 
 int rayt_server_create(rayt_cache* cache, const rayt_server_config* cfg, rayt_server** out);

@@ -81,7 +81,8 @@ class RequestInfo(C.Structure):
 
 class ServerStats(C.Structure):
     _fields_ = [(k, C.c_int64) for k in ["submitted", "completed", "ticks", "rays_traced", "faults",
-                                         "kernel_launches", "bytes_d2h"]]
+                                         "kernel_launches", "bytes_d2h", "uploaded_blocks"]] + [
+        (k, C.c_double) for k in ["host_ms_wait", "host_ms_lru", "host_ms_load"]]
 
 
 class CameraStruct(C.Structure):

@@ -236,9 +236,10 @@ int Cache::Init(Tree* tree, int max_blocks) {
   max_blocks_ = max_blocks > 0 ? max_blocks : (int)tree->info.blocks_count;
   const uint64_t nodes = (uint64_t)max_blocks_ * (uint64_t)nib_;
   // cache-format limits: far pointer slots (index*8+i) must fit in 21 bits;
-  // node indices are int (the reference's per-pixel feedback word
-  // ((node+1)<<1)|dup needs node < 2^30, which only recorded passes build)
-  if (nodes >= (1ull << 31)) return fail(RAYT_E_LIMIT, "cache holds >= 2^31 nodes");
+  // node indices (far pointer values, the traversal's node arithmetic) are
+  // unsigned 32-bit (the reference's per-pixel feedback word ((node+1)<<1)|dup
+  // needs node < 2^30, which only recorded passes build)
+  if (nodes >= (1ull << 32)) return fail(RAYT_E_LIMIT, "cache holds >= 2^32 nodes");
   if ((uint64_t)max_blocks_ * 8 >= (1ull << 21)) return fail(RAYT_E_LIMIT, "cache has >= 2^18 blocks (far pointer index overflows)");
   if (tree->chan_names.size() > (size_t)kMaxChannels) return fail(RAYT_E_LIMIT, "too many channels");
   RAYT_CUDA_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
@@ -351,13 +352,13 @@ void Cache::DropMarker(int k) {
 
 // ---- uploads -------------------------------------------------------------------
 void Cache::AddPatch(bool far_buffer, uint32_t index, uint32_t value) {
-  const uint32_t where = far_buffer ? (0x80000000u | index) : index;
+  const uint64_t where = ((uint64_t)(far_buffer ? 1 : 0) << 32) | index;
   auto it = patch_at_.find(where);
   if (it != patch_at_.end()) {
     patches_[it->second].value = value;  // last write to an address wins
   } else {
     patch_at_[where] = (int)patches_.size();
-    patches_.push_back(Patch{where, value});
+    patches_.push_back(Patch{index, value, far_buffer ? 1u : 0u});
   }
   if (!far_buffer) touched_[index / (uint32_t)nib_] = epoch_;
   ++stats_.pointer_patches;
@@ -618,7 +619,7 @@ int Cache::Place(int pos, std::vector<int>* queue) {
   info.block = block;
   InsertBefore(s, next_[head_]);  // LRU front, then MarkBlockAsUsed
   Touch(s);
-  if (is_root) root_node_ = s * nib_ + root_child;
+  if (is_root) root_node_ = (uint32_t)s * (uint32_t)nib_ + (uint32_t)root_child;
   return RAYT_OK;
 }
 
@@ -780,7 +781,7 @@ void rayt_cache_destroy(rayt_cache* c) { delete C(c); }
 int rayt_cache_initial_fill(rayt_cache* c) { return c ? C(c)->InitialFill() : fail(RAYT_E_ARG, "null cache"); }
 int rayt_cache_root_node_index(const rayt_cache* c, int* out) {
   if (!c || !out) return fail(RAYT_E_ARG, "null argument");
-  *out = C(c)->root_node();
+  *out = (int)C(c)->root_node();  // the node index's 32 bits (unsigned beyond 2^31 - 1)
   return RAYT_OK;
 }
 int rayt_cache_blocks(const rayt_cache* c, int* loaded, int* max_blocks) {

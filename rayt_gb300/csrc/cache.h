@@ -29,7 +29,7 @@ class Cache {
   int EndTransaction();
   int EndSession();
 
-  int root_node() const { return root_node_; }
+  uint32_t root_node() const { return root_node_; }
   int loaded() const { return first_free_; }
   int max_blocks() const { return max_blocks_; }
   int nodes_in_block() const { return nib_; }
@@ -61,7 +61,8 @@ class Cache {
   };
 
   Tree* tree_ = nullptr;
-  int nib_ = 0, max_blocks_ = 0, first_free_ = 0, root_node_ = 0;
+  int nib_ = 0, max_blocks_ = 0, first_free_ = 0;
+  uint32_t root_node_ = 0;   // node index: below 2^32 (caches hold fewer than 2^32 nodes)
   cudaStream_t stream_ = nullptr;
   std::vector<uint8_t*> d_chan_;
   std::vector<int> chan_bytes_;
@@ -100,7 +101,7 @@ class Cache {
   int* h_slots_ = nullptr;       // pinned, per position (-1: staged but not placed)
   int* d_slots_ = nullptr;
   std::vector<Patch> patches_;
-  std::unordered_map<uint32_t, int> patch_at_;
+  std::unordered_map<uint64_t, int> patch_at_;  // (far << 32 | index) -> position in patches_
   Patch* h_patches_ = nullptr;   // pinned, two halves
   Patch* d_patches_ = nullptr;
   int patch_cap_ = 0, patch_half_ = 0;

@@ -58,7 +58,7 @@ struct TraceParams {
   const uint32_t* far_ptrs;
   const char4* normals;    // may be null
   const uchar4* colors;    // may be null
-  int root;
+  uint32_t root;           // node index of the root (cache node indices are unsigned 32-bit)
   int nodes_in_block;
   uint32_t node_limit;     // nodes in the cache (max_blocks * nodes_in_block)
   uint32_t far_limit;      // far pointers in the cache (max_blocks * 8)
@@ -202,8 +202,9 @@ struct UploadParams {
   uint8_t* chan[kMaxChannels]; // channel 0 = node links
 };
 struct Patch {
-  uint32_t where;  // bit 31: far-pointer buffer, else node-link buffer; low bits: index
+  uint32_t index;  // node-link index (below 2^32) or far-pointer index
   uint32_t value;
+  uint32_t far;    // 1: far-pointer buffer, 0: node-link buffer
 };
 cudaError_t launch_upload(const UploadParams& p, cudaStream_t s);
 cudaError_t launch_patches(const Patch* patches, int n, uint32_t* links, uint32_t* far_ptrs, cudaStream_t s);

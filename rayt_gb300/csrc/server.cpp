@@ -395,8 +395,10 @@ int Server::Step(int* finished) {
   RAYT_CUDA_TRY(launch_unique_from_bits(u, s_));
   ++stats.kernel_launches;
   RAYT_CUDA_TRY(cudaMemcpyAsync(h_counts_ + 4, d_client_faults_, kMaxClients * 4, cudaMemcpyDeviceToHost, s_));
+  const double t_sync = now_s();
   RAYT_CUDA_TRY(cudaStreamSynchronize(s_));
   const double t_pass = now_s();
+  stats.host_ms_wait += (t_pass - t_sync) * 1e3;
   stats.rays_traced += rays_tick;
   ++stats.ticks;
   carried_ = h_counts_[2];
@@ -420,6 +422,7 @@ int Server::Step(int* finished) {
   }
 
   // feedback decode and the cache transaction (shared LRU, block streaming)
+  const int64_t uploaded0 = cache_->stats().uploaded_blocks;
   fb_.Decode(h_unique_, h_counts_[0], rand);
   int rc = cache_->StartSession();
   if (rc == RAYT_OK) rc = cache_->StartTransaction();
@@ -430,9 +433,13 @@ int Server::Step(int* finished) {
       if (cache_->TransactionFilled()) break;
       if ((rc = cache_->RequestBlock(b)) != RAYT_OK) break;
     }
+    const double t_lru = now_s();
+    stats.host_ms_lru += (t_lru - t_pass) * 1e3;
     const int erc = cache_->EndTransaction();
+    stats.host_ms_load += (now_s() - t_lru) * 1e3;
     if (rc == RAYT_OK) rc = erc;
   }
+  stats.uploaded_blocks += cache_->stats().uploaded_blocks - uploaded0;
   const bool filled = cache_->in_session() && cache_->SessionFilled();
   if (cache_->in_transaction()) cache_->EndTransaction();
   if (cache_->in_session()) {

@@ -113,7 +113,7 @@ struct Cast {
 // desc.  kFault: node = parent, t = t_min, block = desc >> 11.
 enum Outcome : int { kRunning = 0, kHit = 1, kFault = 2, kMiss = 3, kError = 4 };
 
-__device__ __forceinline__ void cast_begin(Cast& c, int root, float4 o, float4 d) {
+__device__ __forceinline__ void cast_begin(Cast& c, uint32_t root, float4 o, float4 d) {
   float px0 = o.x + 1.0f, py0 = o.y + 1.0f, pz0 = o.z + 1.0f;
   float dx = d.x, dy = d.y, dz = d.z;
   c.coef = d.w;
@@ -135,7 +135,7 @@ __device__ __forceinline__ void cast_begin(Cast& c, int root, float4 o, float4 d
   c.t_max = fminf(fminf(c.tx_coef - c.tx_bias, c.ty_coef - c.ty_bias), c.tz_coef - c.tz_bias);
   c.h = c.t_max;
   c.t_min = fmaxf(c.t_min, 0.0f);
-  c.parent = (uint32_t)root;
+  c.parent = root;
   c.desc = 0;
   c.idx = 0;
   c.px = 1.0f;
@@ -428,20 +428,30 @@ __device__ __forceinline__ int cast_run(Cast& c, int stop, uint2* stack, const T
   return outcome;
 }
 
+// x / 127 correctly rounded for an integer x in [-128, 127] (a char normal
+// component): the product with the rounded reciprocal, then one FMA-exact
+// residual correction.  Equal to the IEEE quotient for all 256 inputs (a CPU
+// test checks every one); a fifth of a full-range division's instructions.
+__device__ __forceinline__ float div127(float x) {
+  const float r = 1.0f / 127.0f;
+  const float q0 = x * r;
+  const float e = fmaf(-q0, 127.0f, x);
+  return fmaf(e, r, q0);
+}
+
 // ProcessHit: fixed ambient + three directional lights; returns RGBA8 (A=255).
-__device__ __forceinline__ uchar4 shade(const TraceParams& p, int node) {
-  // normalize((2,-2,3,0))*.6, normalize((-3,-3,-2,0))*.5, normalize((1,2.5,-1,0))*.3
-  float l[3][3];
-  const float src[3][4] = {{2.f, -2.f, 3.f, .6f}, {-3.f, -3.f, -2.f, .5f}, {1.f, 2.5f, -1.f, .3f}};
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    float len = __fsqrt_rn(dot4(src[k][0], src[k][1], src[k][2], 0.f, src[k][0], src[k][1], src[k][2], 0.f));
-#pragma unroll
-    for (int c = 0; c < 3; ++c) l[k][c] = __fdiv_rn(src[k][c], len) * src[k][3];
-  }
+__device__ __forceinline__ uchar4 shade(const TraceParams& p, uint32_t node) {
   const char4 cn = p.normals[node];
-  const float nx = __fdiv_rn((float)cn.x, 127.f), ny = __fdiv_rn((float)cn.y, 127.f),
-              nz = __fdiv_rn((float)cn.z, 127.f), nw = __fdiv_rn(0.0f, 127.f);
+  // the reference's w component is 0 / 127 = +0
+  const float nx = div127((float)cn.x), ny = div127((float)cn.y), nz = div127((float)cn.z), nw = 0.0f;
+  // The light directions (shading.cl:7-32): normalize(v) * w for v, w =
+  // (2,-2,3), .6; (-3,-3,-2), .5; (1,2.5,-1), .3, each as the reference
+  // computes it per call in IEEE float (dot left to right, correctly rounded
+  // sqrt and divisions, then the product).  Constants, so no ray pays for 3
+  // square roots and 9 divisions; a CPU test recomputes them.
+  const float l[3][3] = {{0x1.2a071ep-2f, -0x1.2a071ep-2f, 0x1.bf0aacp-2f},
+                         {-0x1.4779eep-2f, -0x1.4779eep-2f, -0x1.b4a294p-3f},
+                         {0x1.abd032p-4f, 0x1.0b6220p-2f, -0x1.abd032p-4f}};
   float a[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -598,7 +608,7 @@ __device__ __forceinline__ void end_ray(const TraceParams& p, const RayEnd& e, u
     p.image[ray] = finish(p, make_uchar4(0, 0, 0, 0));
     if (p.depth) write_depth(p, ray, __uint_as_float(kDepthInf), -1);
   } else {
-    const uchar4 col = (p.normals && p.colors) ? shade(p, node) : make_uchar4(0, 0, 0, 0);
+    const uchar4 col = (p.normals && p.colors) ? shade(p, (uint32_t)node) : make_uchar4(0, 0, 0, 0);
     p.image[ray] = finish(p, col);
     word = (int32_t)(((uint32_t)(node + 1) << 1) | (uint32_t)dup);
     if (p.depth) write_depth(p, ray, adv + e.t, node);
@@ -620,7 +630,7 @@ __device__ __forceinline__ void end_ray(const TraceParams& p, const RayEnd& e, u
     if (p.out_adv) p.out_adv[slot] = p.restart ? adv : adv + e.t;
   }
   warp_set_bit(p.fault_bits, faulted && fault_block < p.fault_bit_limit ? fault_block : -1);
-  warp_set_bit(p.hit_bits, hit ? 2 * (node / p.nodes_in_block) + dup : -1);
+  warp_set_bit(p.hit_bits, hit ? (int)(2 * ((uint32_t)node / (uint32_t)p.nodes_in_block)) + dup : -1);
   {
     const unsigned active = __activemask();
     const unsigned m = __ballot_sync(active, word != kNoHit);
@@ -736,7 +746,7 @@ __global__ void __launch_bounds__(kBlockThreads) trace_queue_kernel(const __grid
       if (!kFirst && p.finish_mask && ((p.finish_mask >> slot_of(p, ray)) & 1ull)) {
         // served mode: the request stops here; FinishTracingFrame's shading
         // with the fault's parent node
-        const uchar4 col = (p.normals && p.colors) ? shade(p, p.in_parent[r]) : make_uchar4(0, 0, 0, 0);
+        const uchar4 col = (p.normals && p.colors) ? shade(p, (uint32_t)p.in_parent[r]) : make_uchar4(0, 0, 0, 0);
         p.image[ray] = finish(p, col);
         if (p.depth) write_depth(p, ray, adv, p.in_parent[r]);
       } else {
@@ -754,7 +764,7 @@ __global__ void __launch_bounds__(kBlockThreads) trace_queue_kernel(const __grid
 __global__ void __launch_bounds__(kBlockThreads) finish_kernel(const __grid_constant__ TraceParams p) {
   const int i = blockIdx.x * kBlockThreads + threadIdx.x;
   if (i >= *p.n_in) return;
-  const uchar4 col = (p.normals && p.colors) ? shade(p, p.in_parent[i]) : make_uchar4(0, 0, 0, 0);
+  const uchar4 col = (p.normals && p.colors) ? shade(p, (uint32_t)p.in_parent[i]) : make_uchar4(0, 0, 0, 0);
   p.image[p.in_ray[i]] = finish(p, col);
   if (p.depth) write_depth(p, p.in_ray[i], p.in_adv[i], p.in_parent[i]);
 }

@@ -59,8 +59,8 @@ __global__ void patch_kernel(const Patch* patches, int n, uint32_t* links, uint3
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const Patch q = patches[i];
-  if (q.where & 0x80000000u) far_ptrs[q.where & 0x7fffffffu] = q.value;
-  else links[q.where] = q.value;
+  if (q.far) far_ptrs[q.index] = q.value;
+  else links[q.index] = q.value;
 }
 
 }  // namespace

@@ -141,3 +141,40 @@ def test_served_pass_cap_truncates(trees):
     assert info["truncated"] == 1
     img = srv.read_image(c)
     assert img[..., 3].min() == 255  # every pixel was written
+
+
+def test_served_mix_under_eviction_equals_alone(trees):
+    """A shared cache far smaller than the tree (120 of 790 blocks): the mixed
+    clients' blocks evict one another from the one LRU, and every request that
+    ends without truncation still has the image it has alone and the oracle's
+    resident one-view image (restart semantics).  The eviction happened: more
+    blocks were uploaded than the cache holds."""
+    frames = 3
+    sizes = SIZES[:4]
+    mats = {v: [_matrix(_cam(50.0 * f + 80 * v, v), w, h) for f in range(frames)] for v, (w, h) in enumerate(sizes)}
+    alone = {}
+    for v, (w, h) in enumerate(sizes):
+        ld, cm, srv = _server(trees, max_blocks=120)
+        c = srv.add_client(w, h)
+        for f in range(frames):
+            info = srv.wait(srv.submit(c, mats[v][f]))
+            alone[v, f] = (info["truncated"], srv.read_image(c))
+        srv.close()
+    ld, cm, srv = _server(trees, max_blocks=120)
+    ids = [srv.add_client(w, h) for w, h in sizes]
+    compared = 0
+    for f in range(frames):
+        reqs = [srv.submit(ids[v], mats[v][f]) for v in range(len(sizes))]
+        for v, r in enumerate(reqs):
+            info = srv.wait(r)
+            if info["truncated"] or alone[v, f][0]:
+                continue
+            img = srv.read_image(ids[v])
+            np.testing.assert_array_equal(img, alone[v, f][1], err_msg="client %d frame %d" % (v, f))
+            w, h = sizes[v]
+            np.testing.assert_array_equal(img, _resident(trees, w, h, mats[v][f]), err_msg="oracle %d %d" % (v, f))
+            compared += 1
+    uploaded = cm.stats()["uploaded_blocks"]
+    srv.close()
+    assert compared >= 2
+    assert uploaded > 120  # blocks were evicted and others loaded into their slots

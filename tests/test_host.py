@@ -122,3 +122,38 @@ def test_camera_helper_sweep_matches_reference():
     for i, c in enumerate(cams):
         got[i] = R.Camera(c[0], c[1], c[2], c[3:6], c[6], c[7]).view_proj_inv()
     np.testing.assert_array_equal(got.view(np.uint32), d["matrices"].view(np.uint32))
+
+
+def test_shading_light_constants_are_the_references():
+    """The traversal kernel shades with the three light directions of
+    shading.cl:7-32 as float constants; recomputed here as the reference
+    computes them per call in IEEE float: normalize(v) = v / sqrt(dot(v, v))
+    (dot left to right, correctly rounded sqrt and division), times w."""
+    src = open(os.path.join(ROOT, "rayt_gb300", "csrc", "trace.cu")).read()
+    m = re.search(r"const float l\[3\]\[3\] = \{(.*?)\};", src, re.S)
+    got = [float.fromhex(t.rstrip("f")) for t in re.findall(r"-?0x[0-9a-f.]+p-?\d+f", m.group(1))]
+    f = np.float32
+    want = []
+    for (x, y, z), w in [((2, -2, 3), .6), ((-3, -3, -2), .5), ((1, 2.5, -1), .3)]:
+        x, y, z, w = f(x), f(y), f(z), f(w)
+        d = f(f(f(f(x * x) + f(y * y)) + f(z * z)) + f(f(0) * f(0)))
+        ln = np.sqrt(d, dtype=np.float32)
+        want += [float(f(f(c / ln) * w)) for c in (x, y, z)]
+    assert got == want
+
+
+def test_normal_component_division_identity():
+    """x / 127 for every char normal component x: the kernel's product with the
+    rounded reciprocal plus one fused residual correction equals the IEEE
+    quotient (libm's fmaf stands in for the GPU's fused multiply-add)."""
+    libm = ctypes.CDLL("libm.so.6")
+    fmaf = libm.fmaf
+    fmaf.restype = ctypes.c_float
+    fmaf.argtypes = [ctypes.c_float] * 3
+    f = np.float32
+    r = f(1) / f(127)
+    for x in range(-128, 128):
+        q0 = f(x) * r
+        e = f(fmaf(float(-q0), 127.0, float(x)))
+        q1 = f(fmaf(float(e), float(r), float(q0)))
+        assert q1.view(np.uint32) == (f(x) / f(127)).view(np.uint32), x
