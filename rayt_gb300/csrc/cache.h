@@ -2,6 +2,7 @@
 // device buffers and batched uploads).  See cache.cpp.
 #pragma once
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <chrono>
 #include <cstdint>
 #include <string>
@@ -11,6 +12,61 @@
 #include "tree.h"
 
 namespace rayt {
+
+// Position of each patched address in a batch's patch list: open addressing
+// over 64-bit keys, cleared in O(1) by a generation stamp (the batch's
+// patches are few, so the table stays in L1; std::unordered_map allocated a
+// node per insert).
+class PatchIndex {
+ public:
+  void Clear() {
+    n_ = 0;
+    if (++gen_ == 0) {
+      std::fill(stamp_.begin(), stamp_.end(), 0u);
+      gen_ = 1;
+    }
+  }
+  // The value stored for key, or -1; with insert, stores `value` for a new key.
+  int Find(uint64_t key) const {
+    if (stamp_.empty()) return -1;
+    const size_t mask = stamp_.size() - 1;
+    for (size_t h = Hash(key) & mask;; h = (h + 1) & mask) {
+      if (stamp_[h] != gen_) return -1;
+      if (key_[h] == key) return val_[h];
+    }
+  }
+  void Insert(uint64_t key, int value) {  // key must not be present
+    if (2 * (n_ + 1) > stamp_.size()) Grow();
+    const size_t mask = stamp_.size() - 1;
+    size_t h = Hash(key) & mask;
+    while (stamp_[h] == gen_) h = (h + 1) & mask;
+    stamp_[h] = gen_;
+    key_[h] = key;
+    val_[h] = value;
+    ++n_;
+  }
+
+ private:
+  std::vector<uint64_t> key_;
+  std::vector<int> val_;
+  std::vector<uint32_t> stamp_;
+  uint32_t gen_ = 1;
+  size_t n_ = 0;
+  static size_t Hash(uint64_t k) { return (size_t)((k * 0x9E3779B97F4A7C15ull) >> 20); }
+  void Grow() {
+    std::vector<uint64_t> keys;
+    std::vector<int> vals;
+    for (size_t i = 0; i < stamp_.size(); ++i)
+      if (stamp_[i] == gen_) keys.push_back(key_[i]), vals.push_back(val_[i]);
+    const size_t size = stamp_.empty() ? 1024 : stamp_.size() * 4;
+    key_.assign(size, 0);
+    val_.assign(size, 0);
+    stamp_.assign(size, 0u);
+    gen_ = 1;
+    n_ = 0;
+    for (size_t i = 0; i < keys.size(); ++i) Insert(keys[i], vals[i]);
+  }
+};
 
 class Cache {
  public:
@@ -101,7 +157,7 @@ class Cache {
   int* h_slots_ = nullptr;       // pinned, per position (-1: staged but not placed)
   int* d_slots_ = nullptr;
   std::vector<Patch> patches_;
-  std::unordered_map<uint64_t, int> patch_at_;  // (far << 32 | index) -> position in patches_
+  PatchIndex patch_at_;          // (far << 32 | index) -> position in patches_
   Patch* h_patches_ = nullptr;   // pinned, two halves
   Patch* d_patches_ = nullptr;
   int patch_cap_ = 0, patch_half_ = 0;
@@ -127,6 +183,7 @@ class Cache {
   void StartRead(const int* blocks, int n);
   void FinishRead();
   std::chrono::steady_clock::time_point read_started_;
+  void Warm(int first, int n) const;
   int Place(int pos, std::vector<int>* queue);
   int Unload();
   void AddPatch(bool far_buffer, uint32_t index, uint32_t value);

@@ -198,18 +198,30 @@ __device__ __forceinline__ RayEnd cast_ray(const TraceParams& p, float4 o, float
   if (1.5f * ty_coef - ty_bias > t_min) idx ^= 2, py = 1.5f;
   if (1.5f * tz_coef - tz_bias > t_min) idx ^= 4, pz = 1.5f;
   int iter = 0;
+  // Every parent is the root or a child index checked against node_limit
+  // below, so only the root needs a check (a corrupt cache ends the ray as an
+  // error, like the iteration limit).
+  if (p.root >= p.node_limit) {
+    r.error = 1;
+    r.node = -1;
+    r.t = 0.0f;
+    r.iter = 0;
+    return r;
+  }
+  // The parent's descriptor is fetched where the reference's loop will need
+  // it: here for the root, and at each pop (raycast.cl fetches it at the top
+  // of the next iteration, which always follows a pop; same value, one fewer
+  // test per iteration).  The counting form keeps the reference's fetch
+  // points so its counts equal the oracle's.
+  if (!kCount) desc = __ldg(p.links + parent);
   while (scale < kSMax) {
     if (++iter > kIterLimit) {
       r.error = 1;
       break;
     }
-    if (desc == 0) {
-      if (parent >= p.node_limit) {  // only reachable from a corrupt cache
-        r.error = 1;
-        break;
-      }
+    if (kCount && desc == 0) {
       desc = __ldg(p.links + parent);
-      if (kCount) ++fetches;
+      ++fetches;
     }
     const float tx_corner = px * tx_coef - tx_bias;
     const float ty_corner = py * ty_coef - ty_bias;
@@ -280,6 +292,7 @@ __device__ __forceinline__ RayEnd cast_ray(const TraceParams& p, float4 o, float
       const uint2 e = stack[scale];
       parent = e.x;
       t_max = __uint_as_float(e.y);
+      desc = kCount ? 0u : __ldg(p.links + parent);  // the parent's descriptor, needed next iteration
       const uint32_t shx = __float_as_uint(px) >> scale;
       const uint32_t shy = __float_as_uint(py) >> scale;
       const uint32_t shz = __float_as_uint(pz) >> scale;
@@ -288,7 +301,6 @@ __device__ __forceinline__ RayEnd cast_ray(const TraceParams& p, float4 o, float
       pz = __uint_as_float(shz << scale);
       idx = (int)((shx & 1u) | ((shy & 1u) << 1) | ((shz & 1u) << 2));
       h = 0.0f;
-      desc = 0;
     }
   }
   if (scale >= kSMax && !r.error && r.fault_block == -1) r.node = -1;  // left the octree: miss
