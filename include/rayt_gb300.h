@@ -337,6 +337,7 @@ typedef struct {
   double host_ms_wait;       /* host time blocked on the GPU (tick passes), summed over ticks */
   double host_ms_lru;        /* feedback decode, LRU marks and block requests */
   double host_ms_load;       /* EndTransaction: block reads, placement (evictions), upload issue */
+  double gpu_ms_upload;      /* device time of block uploads (copies, upload and patch kernels) */
 } rayt_server_stats;
 
 int rayt_server_create(rayt_cache* cache, const rayt_server_config* cfg, rayt_server** out);

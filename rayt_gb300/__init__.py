@@ -82,7 +82,7 @@ class RequestInfo(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [(k, C.c_int64) for k in ["submitted", "completed", "ticks", "rays_traced", "faults",
                                          "kernel_launches", "bytes_d2h", "uploaded_blocks"]] + [
-        (k, C.c_double) for k in ["host_ms_wait", "host_ms_lru", "host_ms_load"]]
+        (k, C.c_double) for k in ["host_ms_wait", "host_ms_lru", "host_ms_load", "gpu_ms_upload"]]
 
 
 class CameraStruct(C.Structure):

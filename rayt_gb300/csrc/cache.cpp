@@ -227,6 +227,10 @@ Cache::~Cache() {
     if (e) cudaEventDestroy(e);
   for (auto& e : patch_free_)
     if (e) cudaEventDestroy(e);
+  for (auto& e : flush_ev_) {
+    cudaEventDestroy(e.first);
+    cudaEventDestroy(e.second);
+  }
   if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -370,6 +374,17 @@ void Cache::AddPatch(bool far_buffer, uint32_t index, uint32_t value) {
 int Cache::FlushTo(int end) {
   if (end <= batch_begin_ && patches_.empty()) return RAYT_OK;
   const int h = half_;
+  // device time of the batch: events around its copies and kernels (the
+  // last 256 batches between two TakeUploadMs calls are counted)
+  if (flush_used_ == kFlushEvents) flush_used_ = 0;
+  if (flush_used_ == (int)flush_ev_.size()) {
+    cudaEvent_t a = nullptr, b = nullptr;
+    RAYT_CUDA_TRY(cudaEventCreate(&a));
+    RAYT_CUDA_TRY(cudaEventCreate(&b));
+    flush_ev_.emplace_back(a, b);
+  }
+  const std::pair<cudaEvent_t, cudaEvent_t> ev = flush_ev_[flush_used_++];
+  RAYT_CUDA_TRY(cudaEventRecord(ev.first, stream_));
   if (end > batch_begin_) {
     const size_t first = (size_t)stage_cap_ * h + batch_begin_;
     const int n = end - batch_begin_;
@@ -414,7 +429,20 @@ int Cache::FlushTo(int end) {
   patch_at_.Clear();
   batch_begin_ = std::max(batch_begin_, end);
   ++epoch_;
+  RAYT_CUDA_TRY(cudaEventRecord(ev.second, stream_));
   return RAYT_OK;
+}
+
+// Sum of the device time of the batches flushed since the last call (their
+// copies, upload and patch kernels); the caller has synchronised the stream.
+float Cache::TakeUploadMs() {
+  float total = 0;
+  for (int i = 0; i < flush_used_; ++i) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, flush_ev_[i].first, flush_ev_[i].second) == cudaSuccess) total += ms;
+  }
+  flush_used_ = 0;
+  return total;
 }
 
 // Flushes what is staged and continues in the other half once that half's
@@ -676,6 +704,7 @@ int Cache::InitialFill() {
   }
   if ((rc = FlushTo(staged_)) != RAYT_OK) return rc;
   RAYT_CUDA_TRY(cudaStreamSynchronize(stream_));
+  TakeUploadMs();  // frames report their own uploads, not the fill's
   return RAYT_OK;
 }
 

@@ -100,6 +100,9 @@ class Cache {
   int uploaded_since(int64_t mark) const { return (int)(stats_.uploaded_blocks - mark); }
   bool in_transaction() const { return in_transaction_; }
   bool in_session() const { return in_session_; }
+  // Device time (ms) of the upload batches flushed since the last call: host
+  // to device copies, upload and patch kernels.  Call after a stream sync.
+  float TakeUploadMs();
 
  private:
   static constexpr int kSession = 0, kTransaction = 1, kMarkers = 2;
@@ -169,6 +172,9 @@ class Cache {
 
   rayt_cache_stats stats_{};
   int64_t launches_ = 0;   // upload and patch kernels launched
+  static constexpr int kFlushEvents = 256;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> flush_ev_;  // per flushed batch, reused
+  int flush_used_ = 0;
 
   // list helpers
   void Unlink(int id);

@@ -499,11 +499,9 @@ int Renderer::Frame(const float* m) {
     }
     stats.faults += (int)fb_.faults.size();
     stats.host_ms_decode += ms_since(td);
-    RAYT_CUDA_TRY(cudaEventRecord(ev_[3], s_));
     const auto tl = clock::now();
     const int erc = cache_->EndTransaction();
     stats.host_ms_load += ms_since(tl);
-    RAYT_CUDA_TRY(cudaEventRecord(ev_[4], s_));
     if (rc == RAYT_OK) rc = erc;
     if (rc != RAYT_OK) break;
     active_prev = active_now;
@@ -534,10 +532,7 @@ int Renderer::Frame(const float* m) {
   const auto tw = clock::now();
   RAYT_CUDA_TRY(cudaStreamSynchronize(s_));
   stats.host_ms_wait += ms_since(tw);
-  if (stats.passes > 1 || stats.faults) {
-    float up = 0;
-    if (cudaEventElapsedTime(&up, ev_[3], ev_[4]) == cudaSuccess) ms_up += up;
-  }
+  ms_up += cache_->TakeUploadMs();  // every batch the frame's transactions flushed
   stats.gpu_ms_trace = ms_trace;
   stats.gpu_ms_feedback = ms_fb;
   stats.gpu_ms_upload = ms_up;

@@ -399,6 +399,7 @@ int Server::Step(int* finished) {
   RAYT_CUDA_TRY(cudaStreamSynchronize(s_));
   const double t_pass = now_s();
   stats.host_ms_wait += (t_pass - t_sync) * 1e3;
+  stats.gpu_ms_upload += cache_->TakeUploadMs();  // the previous tick's block uploads
   stats.rays_traced += rays_tick;
   ++stats.ticks;
   carried_ = h_counts_[2];
