@@ -143,24 +143,18 @@ def test_served_pass_cap_truncates(trees):
     assert img[..., 3].min() == 255  # every pixel was written
 
 
-def test_served_mix_under_eviction_equals_alone(trees):
-    """A shared cache far smaller than the tree (120 of 790 blocks): the mixed
-    clients' blocks evict one another from the one LRU, and every request that
-    ends without truncation still has the image it has alone and the oracle's
-    resident one-view image (restart semantics).  The eviction happened: more
-    blocks were uploaded than the cache holds."""
-    frames = 3
-    sizes = SIZES[:4]
-    mats = {v: [_matrix(_cam(50.0 * f + 80 * v, v), w, h) for f in range(frames)] for v, (w, h) in enumerate(sizes)}
+def _mix_under_eviction(trees, max_blocks, sizes, mats, frames):
+    """Requests compared (alone = mixed = oracle) and blocks uploaded, for one
+    shared cache size."""
     alone = {}
     for v, (w, h) in enumerate(sizes):
-        ld, cm, srv = _server(trees, max_blocks=120)
+        ld, cm, srv = _server(trees, max_blocks=max_blocks)
         c = srv.add_client(w, h)
         for f in range(frames):
             info = srv.wait(srv.submit(c, mats[v][f]))
             alone[v, f] = (info["truncated"], srv.read_image(c))
         srv.close()
-    ld, cm, srv = _server(trees, max_blocks=120)
+    ld, cm, srv = _server(trees, max_blocks=max_blocks)
     ids = [srv.add_client(w, h) for w, h in sizes]
     compared = 0
     for f in range(frames):
@@ -170,11 +164,31 @@ def test_served_mix_under_eviction_equals_alone(trees):
             if info["truncated"] or alone[v, f][0]:
                 continue
             img = srv.read_image(ids[v])
-            np.testing.assert_array_equal(img, alone[v, f][1], err_msg="client %d frame %d" % (v, f))
+            np.testing.assert_array_equal(img, alone[v, f][1], err_msg="cache %d client %d frame %d" % (max_blocks, v, f))
             w, h = sizes[v]
-            np.testing.assert_array_equal(img, _resident(trees, w, h, mats[v][f]), err_msg="oracle %d %d" % (v, f))
+            np.testing.assert_array_equal(img, _resident(trees, w, h, mats[v][f]),
+                                          err_msg="cache %d oracle %d %d" % (max_blocks, v, f))
             compared += 1
     uploaded = cm.stats()["uploaded_blocks"]
     srv.close()
-    assert compared >= 2
-    assert uploaded > 120  # blocks were evicted and others loaded into their slots
+    return compared, uploaded
+
+
+def test_served_mix_under_eviction_equals_alone(trees):
+    """A shared cache smaller than the tree (790 blocks): the mixed clients'
+    blocks evict one another from the one LRU, and every request that ends
+    without truncation still has the image it has alone and the oracle's
+    resident one-view image (restart semantics).  Cache sizes are tried from
+    large to small until one both evicts (more blocks uploaded than it holds)
+    and leaves at least two requests untruncated; every untruncated request of
+    every size tried is checked."""
+    frames = 5
+    sizes = SIZES[:3]
+    mats = {v: [_matrix(_cam(72.0 * f + 40 * v, v), w, h) for f in range(frames)] for v, (w, h) in enumerate(sizes)}
+    seen = []
+    for max_blocks in (600, 450, 330, 240):
+        compared, uploaded = _mix_under_eviction(trees, max_blocks, sizes, mats, frames)
+        seen.append((max_blocks, compared, uploaded))
+        if compared >= 2 and uploaded > max_blocks:
+            return
+    raise AssertionError("no cache size both evicted and kept two requests untruncated: %s" % seen)
