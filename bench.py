@@ -812,48 +812,58 @@ def bench_served(args, rank, world, local):
                                                                           cap_blocks))
     fb_bytes = sum(((p + 63) // 64) * 64 * 4 for p in pixels) + (1 << 20)
 
+    state = {"cm": cm}
+
+    def fresh_cache():
+        """Every timed phase starts from the same cache state: a new cache
+        after InitialFillCache (the previous one is released first)."""
+        state["cm"].close()
+        c = R.GPUOctreeCacheManager(cache_blocks(cfg), ld)
+        c.InitialFillCache()
+        state["cm"] = c
+        return c
+
     def make_server(deliver):
-        srv = R.RenderServer(cm, max_clients=nclients, framebuffer_bytes=fb_bytes, max_rays_in_flight=sum(pixels),
-                             max_passes=cfg["max_passes"], lod_voxel_size=cfg["lod"], deliver_to_host=deliver)
+        srv = R.RenderServer(fresh_cache(), max_clients=nclients, framebuffer_bytes=fb_bytes,
+                             max_rays_in_flight=sum(pixels), max_passes=cfg["max_passes"], lod_voxel_size=cfg["lod"],
+                             deliver_to_host=deliver)
         ids = [srv.add_client(w, h) for w, h in sizes]
         return srv, ids
 
     def closed_served(srv, ids, first, frames, cap_s):
-        """Every client keeps one frame outstanding; returns (frames, seconds)."""
-        count = [0] * nclients
-        t_end = time.perf_counter() + cap_s
-
-        def run(c):
-            for f in range(first, first + frames):
-                if time.perf_counter() > t_end:
-                    break
-                srv.wait(srv.submit(ids[c], cams[c][f]), timeout=cap_s + 60)
-                count[c] += 1
-        ts = [threading.Thread(target=run, args=(c,)) for c in range(nclients)]
+        """Closed loop: every client's frames first..first+frames-1 are queued
+        at once; the server admits one request per client at a time, in order,
+        so each client always has its next frame waiting and no host thread's
+        wake-up sits between a client's frames.  Returns (frames, seconds)."""
         srv.start()
         t = time.perf_counter()
-        for th in ts:
-            th.start()
-        for th in ts:
-            th.join()
+        reqs = [srv.submit(ids[c], cams[c][f]) for f in range(first, first + frames) for c in range(nclients)]
+        done = 0
+        for r in reqs:
+            srv.wait(r, timeout=cap_s + 60)
+            done += 1
         el = time.perf_counter() - t
         srv.stop()
-        return sum(count), el
+        return done, el
 
-    srv, ids = make_server(False)
-    closed_served(srv, ids, 0, args.warmup, 60)
-    log("served warm-up done")
+    def served_closed(deliver):
+        srv, ids = make_server(deliver)
+        closed_served(srv, ids, 0, args.warmup, 60)
+        n, el = closed_served(srv, ids, args.warmup, closed_frames, 60)
+        st = srv.stats()
+        srv.close()
+        return n, el, st
+
     barrier(world)
     clocks = ClockSampler(local)
     clocks.start()
-    n_served, el_served = closed_served(srv, ids, args.warmup, closed_frames, 60)
-    st = srv.stats()
-    srv.close()
-    log("served closed loop: %d frames in %.3fs" % (n_served, el_served))
-    srv, ids = make_server(True)
-    n_served_e2e, el_served_e2e = closed_served(srv, ids, args.warmup, closed_frames, 60)
+    n_served, el_served, st = served_closed(False)
+    log("served closed loop: %d frames in %.3fs, %d ticks, %d blocks uploaded" % (n_served, el_served, st["ticks"],
+                                                                                 st["uploaded_blocks"]))
+    n_served_e2e, el_served_e2e, _ = served_closed(True)
     log("served closed loop, delivered to host: %d frames in %.3fs" % (n_served_e2e, el_served_e2e))
     # open loop: the Poisson schedule
+    srv, ids = make_server(True)
     reqs = []
     srv.start()
     t_start = time.perf_counter()
@@ -870,15 +880,22 @@ def bench_served(args, rank, world, local):
     span_served = max(i["done_s"] for i in infos) - min(i["submit_s"] for i in infos)
     log("served open loop: %d requests over %.3fs" % (len(infos), span_served))
 
-    # plain per-frame path: one renderer per client on the same cache
-    rts = []
-    for (w, h) in sizes:
-        rt = R.GPURayTracer(cm, w, h)
-        rt.set_lod_voxel_size(cfg["lod"])
-        rt.set_frame_time_limit(1e30)
-        rt.set_max_passes(cfg["max_passes"])
-        rts.append(rt)
+    # plain per-frame path: one renderer per client on one cache
     pinned = [torch.empty((h, w, 4), dtype=torch.uint8).pin_memory() for w, h in sizes]
+    rts = []
+
+    def plain_renderers():
+        for rt in rts:
+            rt.close()
+        rts.clear()
+        c = fresh_cache()
+        for (w, h) in sizes:
+            rt = R.GPURayTracer(c, w, h)
+            rt.set_lod_voxel_size(cfg["lod"])
+            rt.set_frame_time_limit(1e30)
+            rt.set_max_passes(cfg["max_passes"])
+            rts.append(rt)
+        return c
 
     def plain_frame(c, f, deliver=True):
         rts[c].RenderFrame(cams[c][f])
@@ -886,7 +903,16 @@ def bench_served(args, rank, world, local):
             R._check(R.lib().rayt_renderer_read_image(rts[c]._h, pinned[c].data_ptr(), pinned[c].numel()))
 
     def closed_plain(deliver, cap_s):
+        """The same frames in the same order, one RenderFrame each, from the
+        same cache state (fresh cache, the same warm-up frames)."""
+        pc = plain_renderers()
+        up0 = pc.stats()["uploaded_blocks"]
+        for f in range(args.warmup):
+            for c in range(nclients):
+                plain_frame(c, f, deliver)
+        torch.cuda.synchronize()
         n, t_end = 0, time.perf_counter() + cap_s
+        up1 = pc.stats()["uploaded_blocks"]
         t = time.perf_counter()
         for f in range(args.warmup, args.warmup + closed_frames):
             if time.perf_counter() > t_end:
@@ -895,15 +921,13 @@ def bench_served(args, rank, world, local):
                 plain_frame(c, f, deliver)
                 n += 1
         torch.cuda.synchronize()
-        return n, time.perf_counter() - t
+        return n, time.perf_counter() - t, pc.stats()["uploaded_blocks"] - up1
 
-    for c in range(nclients):
-        for f in range(args.warmup):
-            plain_frame(c, f)
-    n_plain, el_plain = closed_plain(False, 60)
-    n_plain_e2e, el_plain_e2e = closed_plain(True, 60)
-    log("plain closed loop: %d frames in %.3fs (%d in %.3fs delivered)" % (n_plain, el_plain, n_plain_e2e,
-                                                                           el_plain_e2e))
+    n_plain, el_plain, up_plain = closed_plain(False, 60)
+    n_plain_e2e, el_plain_e2e, _ = closed_plain(True, 60)
+    log("plain closed loop: %d frames in %.3fs, %d blocks uploaded (%d in %.3fs delivered)"
+        % (n_plain, el_plain, up_plain, n_plain_e2e, el_plain_e2e))
+    plain_renderers()
     lat_plain = []
     t_start = time.perf_counter()
     for (t, c, f) in sched:
@@ -964,6 +988,7 @@ def bench_served(args, rank, world, local):
                                  "ticks": int(sst["ticks"])}},
         "plain": {"closed_loop_frames_s": round(n_plain / el_plain, 2),
                   "closed_loop_e2e_frames_s": round(n_plain_e2e / el_plain_e2e, 2),
+                  "closed_loop_uploaded_blocks": int(up_plain),
                   "closed_loop_mrays_s": round(n_plain * mean_px / el_plain / 1e6, 1),
                   "open_loop": {"frames_s": round(len(lat_plain) / span_plain, 1), "p50_ms": pp50, "p99_ms": pp99,
                                 "served_requests": len(lat_plain)}},

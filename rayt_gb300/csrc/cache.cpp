@@ -575,28 +575,6 @@ void Cache::FinishRead() {
   stats_.io_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - read_started_).count();
 }
 
-// The staged records of positions [first, first + n) were written by the
-// reading threads, so each one's cache lines sit in another core's cache:
-// placing them one after another paid those transfers one at a time (about
-// 0.65 us of a 0.85 us placement).  Requesting them all up front overlaps the
-// transfers: the records first, then what Place reads through them (the
-// fault-child lists and the parent slot of each block).
-void Cache::Warm(int first, int n) const {
-  const size_t base = (size_t)stage_cap_ * half_ + first;
-  for (int k = 0; k < n; ++k) {
-    const char* m = reinterpret_cast<const char*>(&meta_[base + k]);
-    for (size_t off = 0; off < sizeof(Staged); off += 64) __builtin_prefetch(m + off);
-  }
-  for (int k = 0; k < n; ++k) {
-    const Staged& m = meta_[base + k];
-    if (m.block >= 0) {
-      __builtin_prefetch(&parent_slot_[m.block]);
-      __builtin_prefetch(&block_slot_[m.block]);
-    }
-    if (!m.faults.empty()) __builtin_prefetch(m.faults.data());
-  }
-}
-
 // UploadBlock (gpu-octree-cache.cpp:102-234) for the block staged at `pos`;
 // with a queue, its fault children are appended in InitialFillCache's
 // breadth-first order.
@@ -698,7 +676,6 @@ int Cache::InitialFill() {
     if (chunk.empty()) break;
     const int first = staged_;
     if ((rc = Prefetch(chunk.data(), (int)chunk.size())) != RAYT_OK) return rc;
-    Warm(first, (int)chunk.size());
     for (int i = 0; i < (int)chunk.size() && first_free_ < max_blocks_; ++i)
       if ((rc = Place(first + i, &queue)) != RAYT_OK) return rc;
   }
@@ -776,7 +753,6 @@ int Cache::EndTransaction() {
     chunk_first = -1;
     if (!filled && !TransactionFilled()) start_chunk();  // read ahead while placing
     t = clock::now();
-    Warm(first, n);
     for (int k = 0; k < n && !filled; ++k) {
       if (TransactionFilled()) {
         filled = true;

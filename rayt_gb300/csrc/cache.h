@@ -189,7 +189,6 @@ class Cache {
   void StartRead(const int* blocks, int n);
   void FinishRead();
   std::chrono::steady_clock::time_point read_started_;
-  void Warm(int first, int n) const;
   int Place(int pos, std::vector<int>* queue);
   int Unload();
   void AddPatch(bool far_buffer, uint32_t index, uint32_t value);
