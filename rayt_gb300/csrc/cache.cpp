@@ -283,7 +283,10 @@ int Cache::Init(Tree* tree, int max_blocks) {
   block_slot_.assign(tree->info.blocks_count, -1);
   parent_slot_.assign(tree->info.blocks_count, -1);
   validated_.assign(tree->info.blocks_count, 0);
-  touched_.assign((size_t)max_blocks_, 0);
+  written_.assign((size_t)max_blocks_, 0);
+  written_pos_.assign((size_t)max_blocks_, -1);
+  patched_.assign((size_t)max_blocks_, 0);
+  patch_head_.assign((size_t)max_blocks_, -1);
   const int ids = max_blocks_ + kMarkers + 1;
   prev_.assign(ids, -1);
   next_.assign(ids, -1);
@@ -360,11 +363,21 @@ void Cache::AddPatch(bool far_buffer, uint32_t index, uint32_t value) {
   const int at = patch_at_.Find(where);
   if (at >= 0) {
     patches_[at].value = value;  // last write to an address wins
+    patch_dead_[at] = 0;         // (after any newer content of its slot)
   } else {
-    patch_at_.Insert(where, (int)patches_.size());
+    const int pos = (int)patches_.size();
+    patch_at_.Insert(where, pos);
     patches_.push_back(Patch{index, value, far_buffer ? 1u : 0u});
+    patch_dead_.push_back(0);
+    int next = -1;
+    if (!far_buffer) {  // chain the slot's link patches of this batch
+      const uint32_t s = index / (uint32_t)nib_;
+      if (patched_[s] == epoch_) next = patch_head_[s];
+      patched_[s] = epoch_;
+      patch_head_[s] = pos;
+    }
+    patch_next_.push_back(next);
   }
-  if (!far_buffer) touched_[index / (uint32_t)nib_] = epoch_;
   ++stats_.pointer_patches;
   if (far_buffer) ++stats_.far_pointer_writes;
 }
@@ -408,6 +421,10 @@ int Cache::FlushTo(int end) {
     ++launches_;
     stats_.bytes_h2d += (int64_t)(area_ * n);
   }
+  size_t live = 0;  // patches newer content of their slot did not overwrite, in order
+  for (size_t i = 0; i < patches_.size(); ++i)
+    if (!patch_dead_[i]) patches_[live++] = patches_[i];
+  patches_.resize(live);
   size_t done = 0;
   while (done < patches_.size()) {
     const size_t n = std::min(patches_.size() - done, (size_t)patch_cap_);
@@ -426,6 +443,8 @@ int Cache::FlushTo(int end) {
     done += n;
   }
   patches_.clear();
+  patch_dead_.clear();
+  patch_next_.clear();
   patch_at_.Clear();
   batch_begin_ = std::max(batch_begin_, end);
   ++epoch_;
@@ -596,15 +615,16 @@ int Cache::Place(int pos, std::vector<int>* queue) {
   } else {
     s = first_free_++;
   }
-  if (touched_[s] == epoch_) {
-    // The slot was written or patched earlier in this batch: a batch applies
-    // all block contents before all patches, so submit the batch before this
-    // position (with the eviction's restore patches) first.
-    int rc = FlushTo(pos);
-    if (rc != RAYT_OK) return rc;
-  }
-  h_slots_[(size_t)stage_cap_ * half_ + pos] = s;
-  touched_[s] = epoch_;
+  // This content overwrites the whole slot: an older content of the slot in
+  // this batch is not uploaded, and the batch's earlier patches into the
+  // slot's links are dropped (the sequential order would overwrite both).
+  const size_t spos = (size_t)stage_cap_ * half_ + pos;
+  if (written_[s] == epoch_) h_slots_[written_pos_[s]] = -1;
+  if (patched_[s] == epoch_)
+    for (int q = patch_head_[s]; q >= 0; q = patch_next_[q]) patch_dead_[q] = 1;
+  written_[s] = epoch_;
+  written_pos_[s] = (int)spos;
+  h_slots_[spos] = s;
 
   Slot& info = slots_[s];
   for (uint32_t ptr : m.faults) {

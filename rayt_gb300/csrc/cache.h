@@ -159,13 +159,24 @@ class Cache {
   std::vector<Staged> meta_;     // per position, both halves
   int* h_slots_ = nullptr;       // pinned, per position (-1: staged but not placed)
   int* d_slots_ = nullptr;
+  // A batch applies every block content, then every patch (the last value per
+  // address).  A slot may take new content several times in one batch (evicted
+  // and reused): the newest content supersedes the older staged ones (their
+  // positions are skipped) and patches into the slot's links made before it
+  // are dropped, so the batch leaves the slot as the reference's sequential
+  // order would.
   std::vector<Patch> patches_;
+  std::vector<uint8_t> patch_dead_;  // per patch: overwritten by newer content of its slot
+  std::vector<int> patch_next_;      // per link patch: the slot's previous link patch in the batch, -1 none
   PatchIndex patch_at_;          // (far << 32 | index) -> position in patches_
   Patch* h_patches_ = nullptr;   // pinned, two halves
   Patch* d_patches_ = nullptr;
   int patch_cap_ = 0, patch_half_ = 0;
   cudaEvent_t patch_free_[2] = {nullptr, nullptr};
-  std::vector<int> touched_;     // batch epoch in which a slot was written or patched
+  std::vector<int> written_;     // per slot: batch epoch of its newest content
+  std::vector<int> written_pos_; // per slot: staging index (both halves) of that content
+  std::vector<int> patched_;     // per slot: batch epoch of its newest link patch
+  std::vector<int> patch_head_;  // per slot: newest link patch of the batch
   int epoch_ = 1;
   class ReadPool;
   ReadPool* pool_ = nullptr;
