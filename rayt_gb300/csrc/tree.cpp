@@ -6,9 +6,9 @@
 //  * rayt_build_*: BuildOctree (rayt/CPU data/stored-octree-builder.h:40-41)
 //    through block_builder.h with the sources of scene_source.h.
 //  * rayt_camera_view_proj_inv: Camera::ViewProjectionMatrix().Inverse()
-//    (rayt/scene/camera.cpp:23-28, rayt/util/mat.cpp:108-194): the same
-//    view-projection (horizontal FOV, infinite far plane, y up) inverted in
-//    double precision; see Inverse() below for why it is not bit-identical.
+//    (rayt/scene/camera.cpp:23-28, rayt/util/mat.cpp:20-194): the same float
+//    view-projection (horizontal FOV, infinite far plane, y up) inverted by
+//    the reference's float cofactor method, so the 16 floats are its own.
 #include <algorithm>
 #include <cerrno>
 #include <cstdlib>
