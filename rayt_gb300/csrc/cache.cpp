@@ -138,11 +138,22 @@ class Cache::ReadPool {
   }
   void Wait() {
     if (!fn_) return;
-    const int mine = Work(job_, n_);
+    const int mine = Work(job_, n_) + helped_;
+    helped_ = 0;
     std::unique_lock<std::mutex> lock(mu_);
     done_ += mine;
     done_cv_.wait(lock, [this] { return done_ == n_ && active_ == 0; });
     fn_ = nullptr;
+  }
+  // Between Start() and Wait(), on the thread that called Start(): runs the
+  // job's next unclaimed item, if any (false when all are claimed).
+  bool RunOne() {
+    if (!fn_) return false;
+    const int i = next_.fetch_add(1);
+    if (i >= n_) return false;
+    job_(i);
+    ++helped_;
+    return true;
   }
 
  private:
@@ -153,6 +164,7 @@ class Cache::ReadPool {
   std::function<void(int)> job_;
   const std::function<void(int)>* fn_ = nullptr;  // &job_ while a job runs
   int n_ = 0, done_ = 0, active_ = 0;
+  int helped_ = 0;  // items the starting thread ran through RunOne()
   uint64_t gen_ = 0;
   std::atomic<uint64_t> gen_seen_{0};  // gen_, readable without the lock
   Clock::time_point spin_until_{};
@@ -268,6 +280,8 @@ int Cache::Init(Tree* tree, int max_blocks) {
   for (auto& e : stage_free_) RAYT_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   for (auto& e : patch_free_) RAYT_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   meta_.resize((size_t)stage_cap_ * 2);
+  ready_.reset(new std::atomic<uint8_t>[(size_t)stage_cap_ * 2]);
+  for (size_t k = 0; k < (size_t)stage_cap_ * 2; ++k) ready_[k].store(0, std::memory_order_relaxed);
   patch_cap_ = stage_cap_ * 32 + 64;
   if (cudaHostAlloc(&h_patches_, sizeof(Patch) * patch_cap_ * 2, cudaHostAllocDefault) != cudaSuccess ||
       cudaMalloc(&d_patches_, sizeof(Patch) * patch_cap_ * 2) != cudaSuccess)
@@ -584,9 +598,16 @@ int Cache::Prefetch(const int* blocks, int n) {
 // may place earlier positions meanwhile (reads touch only their positions).
 void Cache::StartRead(const int* blocks, int n) {
   const int first = staged_;
+  const size_t base = (size_t)stage_cap_ * half_ + first;
   read_started_ = std::chrono::steady_clock::now();
-  pool_->Start(n, [this, first, blocks](int i) { ReadOne(first + i, blocks[i]); });
-  for (int i = 0; i < n; ++i) h_slots_[(size_t)stage_cap_ * half_ + first + i] = -1;
+  for (int i = 0; i < n; ++i) {
+    h_slots_[base + i] = -1;
+    ready_[base + i].store(0, std::memory_order_relaxed);
+  }
+  pool_->Start(n, [this, first, base, blocks](int i) {
+    if (!cancel_reads_.load(std::memory_order_relaxed)) ReadOne(first + i, blocks[i]);
+    ready_[base + i].store(1, std::memory_order_release);
+  });
   staged_ += n;
 }
 void Cache::FinishRead() {
@@ -747,48 +768,45 @@ int Cache::RequestBlock(int block) {
 // kReadChunk blocks while this thread places the current one.
 int Cache::EndTransaction() {
   if (!in_transaction_) return fail(RAYT_E_STATE, "no open transaction");
-  constexpr int kReadChunk = 64;
   int rc = RAYT_OK;
-  size_t i = 0;          // next pending block to read
-  bool filled = false;
-  int chunk_first = -1;  // staging position of the chunk being read, -1: none
-  int chunk_n = 0;
-  auto start_chunk = [&]() {
-    if (i >= pending_.size() || staged_ == stage_cap_) return;
-    const int n = (int)std::min<size_t>({(size_t)kReadChunk, (size_t)(stage_cap_ - staged_), pending_.size() - i});
-    chunk_first = staged_;
-    chunk_n = n;
-    StartRead(pending_.data() + i, n);
-    i += n;
-  };
+  size_t i = 0;  // next pending block to stage
+  bool filled = TransactionFilled();
   using clock = std::chrono::steady_clock;
   auto secs = [](clock::time_point a) { return std::chrono::duration<double>(clock::now() - a).count(); };
-  if (!pending_.empty() && staged_ == stage_cap_) rc = NextHalf();
-  if (rc == RAYT_OK && !TransactionFilled()) start_chunk();
-  while (rc == RAYT_OK && chunk_first >= 0) {
-    auto t = clock::now();
-    FinishRead();
-    stats_.io_wait_seconds += secs(t);
-    const int first = chunk_first, n = chunk_n;
-    chunk_first = -1;
-    if (!filled && !TransactionFilled()) start_chunk();  // read ahead while placing
-    t = clock::now();
-    for (int k = 0; k < n && !filled; ++k) {
+  // One read job per staging half: the pool reads the half's blocks in
+  // request order (each position flagged ready when its read is done) while
+  // this thread places them in the same order as soon as each is ready,
+  // helping with unclaimed reads while it waits.  No barrier between groups of
+  // reads; reads not started when the transaction fills the cache are skipped.
+  while (rc == RAYT_OK && !filled && i < pending_.size()) {
+    if (staged_ == stage_cap_ && (rc = NextHalf()) != RAYT_OK) break;
+    const int first = staged_;
+    const int n = (int)std::min<size_t>((size_t)(stage_cap_ - staged_), pending_.size() - i);
+    const size_t base = (size_t)stage_cap_ * half_ + first;
+    StartRead(pending_.data() + i, n);
+    i += (size_t)n;
+    const auto t_loop = clock::now();
+    double waited = 0;
+    for (int k = 0; k < n; ++k) {
+      if (!ready_[base + k].load(std::memory_order_acquire)) {
+        const auto tw = clock::now();
+        while (!ready_[base + k].load(std::memory_order_acquire))
+          if (!pool_->RunOne()) std::this_thread::yield();
+        waited += secs(tw);
+      }
       if (TransactionFilled()) {
         filled = true;
         break;
       }
-      if (block_slot_[meta_[(size_t)stage_cap_ * half_ + first + k].block] >= 0) continue;
+      if (block_slot_[meta_[base + k].block] >= 0) continue;
       if ((rc = Place(first + k, nullptr)) != RAYT_OK) break;
     }
-    stats_.place_seconds += secs(t);
-    if (rc != RAYT_OK || filled) break;
-    if (chunk_first < 0 && i < pending_.size()) {  // the half is full: continue in the other one
-      if ((rc = NextHalf()) != RAYT_OK) break;
-      start_chunk();
-    }
+    stats_.io_wait_seconds += waited;
+    stats_.place_seconds += secs(t_loop) - waited;
+    if (filled || rc != RAYT_OK) cancel_reads_.store(true, std::memory_order_relaxed);
+    FinishRead();
+    cancel_reads_.store(false, std::memory_order_relaxed);
   }
-  if (chunk_first >= 0) FinishRead();  // a read-ahead the transaction no longer needs
   pending_.clear();
   const auto tf = clock::now();
   const int frc = FlushTo(staged_);

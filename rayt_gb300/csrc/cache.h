@@ -3,8 +3,10 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -157,6 +159,9 @@ class Cache {
   int stage_cap_ = 0, half_ = 0, staged_ = 0, batch_begin_ = 0;
   cudaEvent_t stage_free_[2] = {nullptr, nullptr};
   std::vector<Staged> meta_;     // per position, both halves
+  // per position, both halves: 1 once its read finished (or was skipped)
+  std::unique_ptr<std::atomic<uint8_t>[]> ready_;
+  std::atomic<bool> cancel_reads_{false};  // reads not started yet are skipped
   int* h_slots_ = nullptr;       // pinned, per position (-1: staged but not placed)
   int* d_slots_ = nullptr;
   // A batch applies every block content, then every patch (the last value per
