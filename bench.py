@@ -1130,7 +1130,11 @@ def bench_c2(args, rank, world, local):
     peak, kind = hbm_peak()
     if rank != 0:
         return None
-    traffic = profile_traffic("sort_c2")
+    if bitmap:  # the bitmap path's profile was taken at 2^26 and scaled to 2^28 in the summary
+        traffic, traffic_rule = (profile_traffic("sort_c2"), "profiled at 2^26 words, x4") if n == 1 << 28 else \
+            (None, "no profile at this size")
+    else:
+        traffic, traffic_rule = scaled_traffic("sort_c2r", alg)
     # CPU baseline: the reference's merge sort + Hillis-Steele scan pipeline
     # (oracle) on a 2^22-word sample of the same words
     from oracle import oracle as O
@@ -1152,7 +1156,7 @@ def bench_c2(args, rank, world, local):
             "e2e": {"value": round(n * steps / t_e2e / 1e9, 4), "unit": "Gkeys/s", "h2d_bytes_per_step": 4 * n,
                     "d2h_bytes_per_step": 4 * cnt},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(achieved / peak, 4), "traffic": traffic if n == 1 << 28 else None,
+                         "frac": round(achieved / peak, 4), "traffic": traffic, "traffic_rule": traffic_rule,
                          "peak_source": kind,
                          "kernel": ("compaction + range partition + bucket bitmaps + bitmap unique (one call)" if bitmap
                                     else "compaction + 4 digit passes + unique (one call)")},
