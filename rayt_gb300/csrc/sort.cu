@@ -19,14 +19,17 @@
 //                    bitmap in shared memory (so frequent keys cost no global
 //                    atomics), bitmap_unique writes the set bits in order,
 //   radix path       (wider ranges, and GPUSort) four stable digit_kernel
-//                    passes (tiles of 4096 keys, warp ballot ranking,
-//                    per-digit decoupled look-back, scatter staged through
-//                    shared memory) and unique_kernel (run starts counted per
-//                    tile with a look-back prefix).
+//                    passes (persistent CTAs, tiles of 8192 keys brought into
+//                    shared memory by bulk async copies a tile ahead, ranking
+//                    through per-warp peer masks in shared memory, per-digit
+//                    decoupled look-back, scatter staged through shared
+//                    memory) and unique_kernel (run starts counted per tile
+//                    with a look-back prefix).
 // The kernels of the path not taken return at once.  Tiles are claimed in
-// order from an atomic counter, by one CTA per tile (GPUSort, the scan) or by
-// persistent CTAs until the device-side count runs out (feedback unique), so a
-// tile only waits on tiles claimed by running CTAs.  The sort's look-back words
+// order from an atomic counter, by one CTA per tile (the scan) or by
+// persistent CTAs until the device-side count runs out (the digit passes,
+// feedback unique), so a tile only waits on tiles claimed by running CTAs.
+// The sort's look-back words
 // are tagged with a per-call epoch and the pass, so its table is never
 // cleared.  Every wait is bounded and sets an error flag instead of hanging.
 #include <algorithm>
@@ -115,6 +118,7 @@ __device__ uint32_t look_back(const unsigned long long* status, int tile, int st
           atomicExch(&g_error_flag, 1);
           return excl;
         }
+        __nanosleep(32);  // a polling warp yields its issue slots to the SM's other warps
         w[i] = ld_volatile64(status + (size_t)(j - i) * stride + lane);
       }
       excl += (uint32_t)w[i];
@@ -411,115 +415,196 @@ __global__ void hist_offsets_kernel(uint32_t* hist, const int* count, uint32_t* 
   if (threadIdx.x == 0) g_epoch = (g_epoch + 1) & ((1u << 27) - 1);
 }
 
-// The lanes of the warp holding the same 8-bit digit d (a lane whose key is
-// not valid is alone): one ballot per digit bit.  On uniform digits this was
-// 8-11% faster per sort than __match_any_sync; on the Zipf-skewed range
-// buckets of feedback, where few distinct values share a warp,
-// __match_any_sync is faster (2.5x in the range histogram), so those kernels
-// keep it.
-__device__ __forceinline__ unsigned digit_peers(uint32_t d, bool ok) {
-  unsigned peers = __ballot_sync(0xffffffffu, ok);
-  peers = ok ? peers : (1u << (threadIdx.x & 31));
-#pragma unroll
-  for (int b = 0; b < 8; ++b) {
-    const bool bit = (d >> b) & 1u;
-    const unsigned m = __ballot_sync(0xffffffffu, bit);
-    peers &= bit ? m : ~m;
+// ---- bulk async copies into shared memory ------------------------------------
+// A tile of keys arrives in shared memory by one cp.async.bulk (the copy
+// engine moves it; no thread holds it in registers), and its completion is an
+// mbarrier phase with a transaction count.
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+}
+// Makes the barriers' initialisation visible to the copy engine.
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// Waits for the phase of `bar` with parity `parity`; false (error flag set)
+// when the wait runs out.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  long long spins = 0;
+  const unsigned long long start = global_ns();
+  while (!mbar_try_wait(bar, parity)) {
+    if (wait_over(spins, start)) {
+      atomicExch(&g_error_flag, 1);
+      return false;
+    }
   }
-  return peers;
+  return true;
+}
+// Copies `bytes` (a multiple of 16, both addresses 16-byte aligned) from
+// global to shared memory; the copy completes the current phase of `bar`.
+// Shared memory last touched by the threads is handed to the copy engine by
+// the proxy fence.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, unsigned long long* bar) {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
 }
 
 // ---- one stable counting pass over 8 bits ------------------------------------
-// Tiles are claimed in order from tile_counter.  Two launch forms:
-// - one CTA per tile (`persistent` false, GPUSort, where n is known on the
-//   host): measured 12-20% faster than the persistent form;
-// - persistent (feedback unique, whose key count is known only on the device
-//   and whose digit passes must return cheaply when the bitmap path is taken):
-//   the resident CTAs claim tiles until the keys run out; a CTA claims its
-//   next tile when it starts the current one and loads the next tile's keys
-//   once the current keys are ranked and parked in shared memory.  (A next
-//   tile is always above its CTA's current one, so the lowest unfinished tile
-//   is always some CTA's current tile and every look-back ends.)
-// With `range` (feedback unique), skipped on the bitmap path.
-__global__ void __launch_bounds__(kThreads, 4) digit_kernel(const uint32_t* in, uint32_t* out, const int* count,
-                                                         int shift, const uint32_t* digit_base,
-                                                         unsigned long long* status, int* tile_counter, int pass,
-                                                         bool last, int32_t* final_out, const uint32_t* range,
-                                                         bool persistent) {
-  __shared__ uint32_t s_keys[kTile];             // the tile in tile-local sorted order
-  __shared__ uint32_t s_in[kTile];               // the tile as loaded
-  __shared__ uint32_t s_warp[kWarps][kBuckets];
-  __shared__ uint32_t s_tile_start[kBuckets];   // tile-local start of each digit run
-  __shared__ uint32_t s_global[kBuckets];       // global position of each digit run
-  __shared__ int s_tile;
+// Persistent CTAs of 512 threads claim tiles of 8192 keys in order from
+// tile_counter until the keys run out (the count is read on the device: for
+// feedback unique only the compaction knows it).  A CTA claims its next tile
+// when it starts the current one, and the next tile's keys come into the
+// other half of a double buffer by one bulk async copy while the current tile
+// is ranked, looked back and written out.  (A next tile is always above its
+// CTA's current one, so the lowest unfinished tile is always some CTA's
+// current tile and every look-back ends.)  Per tile:
+// - ranking (stable), a warp's 512 keys in 16 rounds of 32: the lanes of a
+//   round holding the same digit find one another through a per-warp table of
+//   peer masks in shared memory (each lane ORs its bit into its digit's word;
+//   one shared atomic instead of eight ballots and the selects between them,
+//   which had made the pass issue-bound at 4.9 warp instructions per key); the
+//   group's first lane adds the group to the warp's count of that digit with
+//   one atomic, clears the mask word and shares the old count; ranks follow
+//   lane order inside the group, and rounds apply in order;
+// - the per-digit counts over warps become offsets; the tile's count per digit
+//   is published at once (the look-back's aggregate); one warp scans the 256
+//   counts into the tile-local start of each digit run;
+// - the keys (held in registers since the ranking) are staged in tile-local
+//   sorted order in place, in the buffer they came from;
+// - one thread per digit looks back for the digit run's global position;
+// - each digit run goes out contiguously.
+// 8192-key tiles halve the look-back's walk per key twice over 4096-key ones:
+// half the tiles, and half as many tiles in flight behind a tile's
+// predecessors.  With `range` (feedback unique), skipped on the bitmap path.
+constexpr int kDigitThreads = 512;
+constexpr int kDigitWarps = kDigitThreads / 32;
+constexpr int kDigitTile = kDigitThreads * kItems;  // 8192 keys
+// shared memory: two tile buffers, per-warp counts and peer masks, the run
+// starts and offsets, two mbarriers and the next tile's index
+constexpr int kDigitSmemBytes = (2 * kDigitTile + 2 * kDigitWarps * kBuckets + 2 * kBuckets) * 4 + 32;
+
+// Bytes copied for tile t of m keys: the partial last tile is rounded up to 16
+// bytes (the key buffers carry 16 bytes of padding).
+__device__ __forceinline__ uint32_t digit_tile_bytes(int t, int m) {
+  const int valid = min(kDigitTile, m - t * kDigitTile);
+  return (uint32_t)((valid * 4 + 15) & ~15);
+}
+
+template <bool kFull>
+__device__ __forceinline__ void rank_tile(const uint32_t* s_tile_keys, uint32_t (&keys)[kItems],
+                                          uint32_t (&ranks)[kItems / 2], uint32_t* s_count, uint32_t* s_peers,
+                                          int shift, int valid, int w0, int lane) {
+#pragma unroll
+  for (int r = 0; r < kItems; ++r) {
+    const int li = w0 + r * 32 + lane;
+    const bool ok = kFull || li < valid;
+    keys[r] = s_tile_keys[li];  // past `valid` a stale word, not used
+    const uint32_t d = (keys[r] >> shift) & 255u;
+    if (ok) atomicOr(&s_peers[d], 1u << lane);
+    __syncwarp();
+    const unsigned peers = ok ? s_peers[d] : (1u << lane);
+    __syncwarp();  // every lane has read its mask before the leader clears it
+    const int leader = __ffs(peers) - 1;
+    uint32_t before = 0;
+    if (ok && lane == leader) {
+      s_peers[d] = 0u;
+      before = atomicAdd(&s_count[d], (uint32_t)__popc(peers));
+    }
+    before = __shfl_sync(0xffffffffu, before, leader);
+    const uint32_t rank = before + __popc(peers & ((1u << lane) - 1));
+    ranks[r / 2] = (r & 1) ? ranks[r / 2] | (rank << 16) : rank;  // two 16-bit ranks (< 512) per word
+  }
+}
+
+__global__ void __launch_bounds__(kDigitThreads, 2) digit_kernel(const uint32_t* in, uint32_t* out, const int* count,
+                                                              int shift, const uint32_t* digit_base,
+                                                              unsigned long long* status, int* tile_counter, int pass,
+                                                              bool last, int32_t* final_out, const uint32_t* range) {
+  extern __shared__ __align__(128) uint32_t smem[];
+  uint32_t* s_warp = smem + 2 * kDigitTile;         // [warp][digit] counts, then offsets
+  uint32_t* s_peers = s_warp + kDigitWarps * kBuckets;  // [warp][digit] peer masks of a round
+  uint32_t* s_start = s_peers + kDigitWarps * kBuckets; // tile-local start of each digit run
+  uint32_t* s_off = s_start + kBuckets;                 // global position - tile-local position
+  unsigned long long* s_bar = reinterpret_cast<unsigned long long*>(s_off + kBuckets);
+  int* s_next = reinterpret_cast<int*>(s_bar + 2);
   if (range && range[2] == kBitmapPath) return;
   const int m = *count;
   const uint32_t tag = g_epoch * 8u + (uint32_t)pass;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int w0 = warp * (kItems * 32);  // warp `warp` ranks keys [w0, w0 + 512) of a tile, 32 per round
-
-  if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1);
-  for (int i = threadIdx.x; i < kWarps * kBuckets; i += kThreads) (&s_warp[0][0])[i] = 0;
-  __syncthreads();
-  int tile = s_tile;
-  __syncthreads();  // every thread has read s_tile
-  if ((long long)tile * kTile >= m) return;
-  uint32_t keys[kItems];
-#pragma unroll
-  for (int r = 0; r < kItems; ++r) {
-    const int li = w0 + r * 32 + lane;
-    keys[r] = li < m - tile * kTile ? __ldg(in + tile * kTile + li) : 0u;
+  const int w0 = warp * (kItems * 32);  // warp `warp` ranks keys [w0, w0 + 512) of a tile
+  for (int i = threadIdx.x; i < 2 * kDigitWarps * kBuckets; i += kDigitThreads) s_warp[i] = 0;
+  if (threadIdx.x == 0) {
+    mbar_init(&s_bar[0]);
+    mbar_init(&s_bar[1]);
+    mbar_init_fence();
+    const int t = atomicAdd(tile_counter, 1);
+    *s_next = t;
+    if ((long long)t * kDigitTile < m) bulk_load(smem, in + (size_t)t * kDigitTile, digit_tile_bytes(t, m), &s_bar[0]);
   }
-  for (;;) {
-    const int base = tile * kTile;
-    const int valid = min(kTile, m - base);
-    if (threadIdx.x == 0)  // the next tile, or none: with a grid of one CTA per tile, each takes one
-      s_tile = persistent ? atomicAdd(tile_counter, 1) : 0x7fffffff / kTile;
-
-    // ranking (stable): per round, the lanes holding a digit take consecutive
-    // ranks after the warp's earlier keys of that digit.  The group's first
-    // lane adds the group to the warp's shared count with one atomic and
-    // shares the old count; the next round's atomic is issued after that
-    // shuffle has read this one's result, so rounds apply in order.
-    uint32_t ranks[kItems / 2];  // two 16-bit ranks (< 512) per word
-#pragma unroll
-    for (int r = 0; r < kItems; ++r) {
-      const int li = w0 + r * 32 + lane;
-      const bool ok = li < valid;
-      const uint32_t d = (keys[r] >> shift) & 255u;
-      const unsigned peers = digit_peers(d, ok);
-      const int leader = __ffs(peers) - 1;
-      uint32_t before = 0;
-      if (ok && lane == leader) before = atomicAdd(&s_warp[warp][d], (uint32_t)__popc(peers));
-      before = __shfl_sync(0xffffffffu, before, leader);
-      const uint32_t rank = before + __popc(peers & ((1u << lane) - 1));
-      ranks[r / 2] = (r & 1) ? ranks[r / 2] | (rank << 16) : rank;
-      if (ok) s_in[li] = keys[r];  // parked in shared memory until the staging step
+  __syncthreads();
+  int tile = *s_next;
+  __syncthreads();  // every thread has read s_next before it is rewritten
+  uint32_t phases = 0u;  // bit b: parity of buffer b's next completion
+  int b = 0;
+  while ((long long)tile * kDigitTile < m) {
+    const int valid = min(kDigitTile, m - tile * kDigitTile);
+    uint32_t* s_tile_keys = smem + b * kDigitTile;
+    if (threadIdx.x == 0) *s_next = atomicAdd(tile_counter, 1);  // read after (A)
+    const bool landed = mbar_wait(&s_bar[b], (phases >> b) & 1u);
+    uint32_t keys[kItems], ranks[kItems / 2];
+    if (valid == kDigitTile)
+      rank_tile<true>(s_tile_keys, keys, ranks, s_warp + warp * kBuckets, s_peers + warp * kBuckets, shift, valid, w0,
+                      lane);
+    else
+      rank_tile<false>(s_tile_keys, keys, ranks, s_warp + warp * kBuckets, s_peers + warp * kBuckets, shift, valid,
+                       w0, lane);
+    // (A) every read of this buffer is done.  A wait that ran out (error flag
+    // set) ends the CTA, after its copy has landed (bounded), so that nothing
+    // lands in shared memory after the CTA has left.
+    if (!__syncthreads_and(landed)) {
+      if (threadIdx.x == 0) mbar_wait(&s_bar[b], (phases >> b) & 1u);
+      return;
     }
-    __syncthreads();
-    const int next = s_tile;
-    const long long next_base = (long long)next * kTile;
+    phases ^= 1u << b;
+    const int next = *s_next;
+    if (threadIdx.x == 0 && (long long)next * kDigitTile < m)  // the other buffer was drained before the last tile ended
+      bulk_load(smem + (b ^ 1) * kDigitTile, in + (size_t)next * kDigitTile, digit_tile_bytes(next, m), &s_bar[b ^ 1]);
     // per digit: exclusive prefix over warps and the tile's count; the count
     // is published at once so later tiles' look-backs can pass this one
-    uint32_t tile_count;
-    {
+    uint32_t tile_count = 0;
+    if (threadIdx.x < kBuckets) {
       const int d = threadIdx.x;
       uint32_t run = 0;
 #pragma unroll
-      for (int w = 0; w < kWarps; ++w) {
-        const uint32_t v = s_warp[w][d];
-        s_warp[w][d] = run;
+      for (int w = 0; w < kDigitWarps; ++w) {
+        const uint32_t v = s_warp[w * kBuckets + d];
+        s_warp[w * kBuckets + d] = run;
         run += v;
       }
       tile_count = run;
       st_volatile64(status + (size_t)tile * kBuckets + d, lb_word(tag, tile == 0 ? 2u : 1u, run));
-      s_tile_start[d] = run;  // temporarily the count; scanned below
+      s_start[d] = run;  // temporarily the count; scanned below
     }
-    __syncthreads();
+    __syncthreads();  // (B)
     if (threadIdx.x < 32) {  // exclusive scan of 256 counts by one warp
       uint32_t v[8], sum = 0;
 #pragma unroll
-      for (int k = 0; k < 8; ++k) { v[k] = s_tile_start[lane * 8 + k]; sum += v[k]; }
+      for (int k = 0; k < 8; ++k) { v[k] = s_start[lane * 8 + k]; sum += v[k]; }
       uint32_t incl = sum;
       for (int off = 1; off < 32; off <<= 1) {
         const uint32_t t = __shfl_up_sync(0xffffffffu, incl, off);
@@ -527,52 +612,58 @@ __global__ void __launch_bounds__(kThreads, 4) digit_kernel(const uint32_t* in, 
       }
       uint32_t run = incl - sum;
 #pragma unroll
-      for (int k = 0; k < 8; ++k) { s_tile_start[lane * 8 + k] = run; run += v[k]; }
+      for (int k = 0; k < 8; ++k) { s_start[lane * 8 + k] = run; run += v[k]; }
     }
-    __syncthreads();
-    // stage keys in tile-local sorted order, before the look-back
+    __syncthreads();  // (C)
+    {  // stage keys in tile-local sorted order, in place: every read of the buffer finished before (A)
+      const uint32_t* s_count = s_warp + warp * kBuckets;
 #pragma unroll
-    for (int r = 0; r < kItems; ++r) {
-      const int li = w0 + r * 32 + lane;
-      if (li < valid) {
-        const uint32_t k = s_in[li];
-        const uint32_t d = (k >> shift) & 255u;
-        const uint32_t rank = (r & 1) ? ranks[r / 2] >> 16 : ranks[r / 2] & 0xffffu;
-        s_keys[s_tile_start[d] + s_warp[warp][d] + rank] = k;
+      for (int r = 0; r < kItems; ++r) {
+        const int li = w0 + r * 32 + lane;
+        if (valid == kDigitTile || li < valid) {
+          const uint32_t k = keys[r];
+          const uint32_t d = (k >> shift) & 255u;
+          const uint32_t rank = (r & 1) ? ranks[r / 2] >> 16 : ranks[r / 2] & 0xffffu;
+          s_tile_keys[s_start[d] + s_count[d] + rank] = k;
+        }
       }
-    }
-    // the next tile's keys are in flight during the look-back and write-out
-#pragma unroll
-    for (int r = 0; r < kItems; ++r) {
-      const long long gi = next_base + w0 + r * 32 + lane;
-      keys[r] = gi < m ? __ldg(in + gi) : 0u;
     }
     // global position of each digit run: look-back over earlier tiles
-    {
+    if (threadIdx.x < kBuckets) {
       const int d = threadIdx.x;
-      if (tile == 0) {
-        s_global[d] = digit_base[d];
-      } else {
-        const uint32_t excl = look_back(status, tile, kBuckets, d, tag);
+      uint32_t excl = 0;
+      if (tile != 0) {
+        excl = look_back(status, tile, kBuckets, d, tag);
         st_volatile64(status + (size_t)tile * kBuckets + d, lb_word(tag, 2u, excl + tile_count));
-        s_global[d] = digit_base[d] + excl;
+      }
+      s_off[d] = digit_base[d] + excl - s_start[d];
+    }
+    __syncthreads();  // (D)
+    // contiguous write-out of each digit run; the counts are cleared for the
+    // next tile on the way (the write-out does not read them)
+    for (int i = threadIdx.x; i < kDigitWarps * kBuckets; i += kDigitThreads) s_warp[i] = 0;
+    if (valid == kDigitTile) {
+#pragma unroll
+      for (int k = 0; k < kItems; ++k) {
+        const int i = threadIdx.x + k * kDigitThreads;
+        const uint32_t key = s_tile_keys[i];
+        const uint32_t pos = s_off[(key >> shift) & 255u] + (uint32_t)i;
+        if (pos >= (uint32_t)m) continue;  // only after a look-back gave up (error flag set)
+        if (last && final_out) final_out[pos] = (int32_t)(key ^ 0x80000000u);
+        else out[pos] = key;
+      }
+    } else {
+      for (int i = threadIdx.x; i < valid; i += kDigitThreads) {
+        const uint32_t key = s_tile_keys[i];
+        const uint32_t pos = s_off[(key >> shift) & 255u] + (uint32_t)i;
+        if (pos >= (uint32_t)m) continue;
+        if (last && final_out) final_out[pos] = (int32_t)(key ^ 0x80000000u);
+        else out[pos] = key;
       }
     }
-    __syncthreads();
-    // contiguous write-out of each digit run; s_warp is cleared for the next
-    // tile on the way (the write-out does not read it)
-    for (int i = threadIdx.x; i < kWarps * kBuckets; i += kThreads) (&s_warp[0][0])[i] = 0;
-    for (int i = threadIdx.x; i < valid; i += kThreads) {
-      const uint32_t k = s_keys[i];
-      const uint32_t d = (k >> shift) & 255u;
-      const uint32_t pos = s_global[d] + (uint32_t)i - s_tile_start[d];
-      if (pos >= (uint32_t)m) continue;  // only after a look-back gave up (error flag set)
-      if (last && final_out) final_out[pos] = (int32_t)(k ^ 0x80000000u);
-      else out[pos] = k;
-    }
-    __syncthreads();  // shared state is reused by the next tile
-    if (next_base >= m) return;
+    __syncthreads();  // (E) the buffer, the run starts and offsets and the counts are reused
     tile = next;
+    b ^= 1;
   }
 }
 
@@ -1029,18 +1120,31 @@ int persistent_grid(int n) {
   return std::min(resident, grid_for(n));
 }
 
+// Resident digit_kernel CTAs (two per SM), at most the tiles of n keys.
+int digit_grid(int n) {
+  static int resident = 0;
+  if (!resident) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaFuncSetAttribute(digit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kDigitSmemBytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, digit_kernel, kDigitThreads, kDigitSmemBytes);
+    resident = sms * (per_sm > 0 ? per_sm : 1);
+  }
+  return std::max(1, std::min(resident, (n + kDigitTile - 1) / kDigitTile));
+}
+
 // The four digit passes.  With `range` (feedback unique) they return at once
 // when the bitmap path was chosen.
 cudaError_t run_passes(SortScratchLayout& l, int n, uint32_t*& cur, uint32_t*& other, int32_t* final_out,
                        const uint32_t* range, cudaStream_t s) {
   cudaError_t e;
-  const bool persistent = range != nullptr;  // without a range the key count is n: one CTA per tile
-  const int grid = persistent ? persistent_grid<digit_kernel>(n) : grid_for(n);
+  const int grid = digit_grid(n);
   for (int p = 0; p < kPasses; ++p) {
     const bool last = p == kPasses - 1;
-    digit_kernel<<<grid, kThreads, 0, s>>>(cur, other, l.count, 8 * p, l.hist + p * kBuckets, l.status,
-                                           l.tile_counter + p, p, last, last ? final_out : nullptr, range,
-                                           persistent);
+    digit_kernel<<<grid, kDigitThreads, kDigitSmemBytes, s>>>(cur, other, l.count, 8 * p, l.hist + p * kBuckets,
+                                                              l.status, l.tile_counter + p, p, last,
+                                                              last ? final_out : nullptr, range);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     std::swap(cur, other);
   }
