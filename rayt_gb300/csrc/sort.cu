@@ -482,10 +482,12 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
 //   one atomic, clears the mask word and shares the old count; ranks follow
 //   lane order inside the group, and rounds apply in order;
 // - the per-digit counts over warps become offsets; the tile's count per digit
-//   is published at once (the look-back's aggregate); one warp scans the 256
-//   counts into the tile-local start of each digit run;
+//   is published at once (the look-back's aggregate); the 256 counts are
+//   scanned into the tile-local start of each digit run, which is added into
+//   the per-warp offsets;
 // - the keys (held in registers since the ranking) are staged in tile-local
-//   sorted order in place, in the buffer they came from;
+//   sorted order in place, in the buffer they came from (one shared load of
+//   the warp's offset per key);
 // - one thread per digit looks back for the digit run's global position;
 // - each digit run goes out contiguously.
 // 8192-key tiles halve the look-back's walk per key twice over 4096-key ones:
@@ -495,8 +497,8 @@ constexpr int kDigitThreads = 512;
 constexpr int kDigitWarps = kDigitThreads / 32;
 constexpr int kDigitTile = kDigitThreads * kItems;  // 8192 keys
 // shared memory: two tile buffers, per-warp counts and peer masks, the run
-// starts and offsets, two mbarriers and the next tile's index
-constexpr int kDigitSmemBytes = (2 * kDigitTile + 2 * kDigitWarps * kBuckets + 2 * kBuckets) * 4 + 32;
+// starts and offsets, 8 warp totals, two mbarriers and the next tile's index
+constexpr int kDigitSmemBytes = (2 * kDigitTile + 2 * kDigitWarps * kBuckets + 2 * kBuckets + 8) * 4 + 32;
 
 // Bytes copied for tile t of m keys: the partial last tile is rounded up to 16
 // bytes (the key buffers carry 16 bytes of padding).
@@ -526,6 +528,7 @@ __device__ __forceinline__ void rank_tile(const uint32_t* s_tile_keys, uint32_t 
       before = atomicAdd(&s_count[d], (uint32_t)__popc(peers));
     }
     before = __shfl_sync(0xffffffffu, before, leader);
+    __syncwarp();  // the cleared mask is in place before the next round's ORs
     const uint32_t rank = before + __popc(peers & ((1u << lane) - 1));
     ranks[r / 2] = (r & 1) ? ranks[r / 2] | (rank << 16) : rank;  // two 16-bit ranks (< 512) per word
   }
@@ -540,7 +543,8 @@ __global__ void __launch_bounds__(kDigitThreads, 2) digit_kernel(const uint32_t*
   uint32_t* s_peers = s_warp + kDigitWarps * kBuckets;  // [warp][digit] peer masks of a round
   uint32_t* s_start = s_peers + kDigitWarps * kBuckets; // tile-local start of each digit run
   uint32_t* s_off = s_start + kBuckets;                 // global position - tile-local position
-  unsigned long long* s_bar = reinterpret_cast<unsigned long long*>(s_off + kBuckets);
+  uint32_t* s_wsum = s_off + kBuckets;                  // per digit warp: its digits' counts summed
+  unsigned long long* s_bar = reinterpret_cast<unsigned long long*>(s_wsum + 8);
   int* s_next = reinterpret_cast<int*>(s_bar + 2);
   if (range && range[2] == kBitmapPath) return;
   const int m = *count;
@@ -586,7 +590,9 @@ __global__ void __launch_bounds__(kDigitThreads, 2) digit_kernel(const uint32_t*
       bulk_load(smem + (b ^ 1) * kDigitTile, in + (size_t)next * kDigitTile, digit_tile_bytes(next, m), &s_bar[b ^ 1]);
     // per digit: exclusive prefix over warps and the tile's count; the count
     // is published at once so later tiles' look-backs can pass this one
-    uint32_t tile_count = 0;
+    // The 256 digit threads (8 warps) also scan the tile's counts: within the
+    // warp by shuffles, across warps through the warp totals after (B).
+    uint32_t tile_count = 0, incl = 0;
     if (threadIdx.x < kBuckets) {
       const int d = threadIdx.x;
       uint32_t run = 0;
@@ -598,33 +604,35 @@ __global__ void __launch_bounds__(kDigitThreads, 2) digit_kernel(const uint32_t*
       }
       tile_count = run;
       st_volatile64(status + (size_t)tile * kBuckets + d, lb_word(tag, tile == 0 ? 2u : 1u, run));
-      s_start[d] = run;  // temporarily the count; scanned below
-    }
-    __syncthreads();  // (B)
-    if (threadIdx.x < 32) {  // exclusive scan of 256 counts by one warp
-      uint32_t v[8], sum = 0;
+      incl = run;
 #pragma unroll
-      for (int k = 0; k < 8; ++k) { v[k] = s_start[lane * 8 + k]; sum += v[k]; }
-      uint32_t incl = sum;
       for (int off = 1; off < 32; off <<= 1) {
         const uint32_t t = __shfl_up_sync(0xffffffffu, incl, off);
         if (lane >= off) incl += t;
       }
-      uint32_t run = incl - sum;
+      if (lane == 31) s_wsum[warp] = incl;
+    }
+    __syncthreads();  // (B)
+    // tile-local start of each digit run, folded into the per-warp offsets so
+    // that staging reads one word per key
+    if (threadIdx.x < kBuckets) {
+      const int d = threadIdx.x;
+      uint32_t start = incl - tile_count;
+      for (int k = 0; k < warp; ++k) start += s_wsum[k];
+      s_start[d] = start;
 #pragma unroll
-      for (int k = 0; k < 8; ++k) { s_start[lane * 8 + k] = run; run += v[k]; }
+      for (int w = 0; w < kDigitWarps; ++w) s_warp[w * kBuckets + d] += start;
     }
     __syncthreads();  // (C)
     {  // stage keys in tile-local sorted order, in place: every read of the buffer finished before (A)
-      const uint32_t* s_count = s_warp + warp * kBuckets;
+      const uint32_t* s_pos = s_warp + warp * kBuckets;
 #pragma unroll
       for (int r = 0; r < kItems; ++r) {
         const int li = w0 + r * 32 + lane;
         if (valid == kDigitTile || li < valid) {
           const uint32_t k = keys[r];
-          const uint32_t d = (k >> shift) & 255u;
           const uint32_t rank = (r & 1) ? ranks[r / 2] >> 16 : ranks[r / 2] & 0xffffu;
-          s_tile_keys[s_start[d] + s_count[d] + rank] = k;
+          s_tile_keys[s_pos[(k >> shift) & 255u] + rank] = k;
         }
       }
     }
