@@ -158,6 +158,10 @@ typedef struct {
   double io_wait_seconds;    /* host time a transaction waited for its block reads */
   double place_seconds;      /* host time placing blocks (slot choice, links, patches) */
   double flush_seconds;      /* host time submitting copies and upload kernels */
+  int64_t mapped;            /* 1: the device reads blocks from the block file mapped into
+                                host memory (no host copy); 0: blocks are read with pread
+                                into pinned staging and copied (RAYT_BLOCK_IO=read, or the
+                                file could not be mapped and registered) */
 } rayt_cache_stats;
 int rayt_cache_stats_get(const rayt_cache* cache, rayt_cache_stats* out);
 

@@ -58,7 +58,8 @@ class TerrainParams(C.Structure):
 class CacheStats(C.Structure):
     _fields_ = [("uploaded_blocks", C.c_int64), ("pointer_patches", C.c_int64), ("far_pointer_writes", C.c_int64),
                 ("bytes_h2d", C.c_int64), ("bytes_read", C.c_int64), ("io_seconds", C.c_double),
-                ("io_wait_seconds", C.c_double), ("place_seconds", C.c_double), ("flush_seconds", C.c_double)]
+                ("io_wait_seconds", C.c_double), ("place_seconds", C.c_double), ("flush_seconds", C.c_double),
+                ("mapped", C.c_int64)]
 
 
 class FrameStats(C.Structure):

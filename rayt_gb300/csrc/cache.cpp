@@ -222,6 +222,10 @@ inline uint32_t CacheLink(uint32_t mask, bool fault, bool dup, bool far_flag, ui
 inline uint32_t NearValue(int64_t from, int64_t to) { return (uint32_t)((1 << 20) + (to - from)); }
 constexpr int kStageBlocksMin = 16;
 constexpr size_t kStageBytes = 32u << 20;  // per half
+// Mapped blocks: positions per half.  A half is also the batch a transaction
+// flushes while it places the next one, so that the device's reads of the
+// file overlap the placement.
+constexpr int kMappedStageBlocks = 512;
 }  // namespace
 
 Cache::~Cache() {
@@ -231,9 +235,11 @@ Cache::~Cache() {
   cudaFree(d_far_);
   cudaFree(d_stage_);
   cudaFree(d_slots_);
+  cudaFree(d_blocks_);
   cudaFree(d_patches_);
   cudaFreeHost(h_stage_);
   cudaFreeHost(h_slots_);
+  cudaFreeHost(h_blocks_);
   cudaFreeHost(h_patches_);
   for (auto& e : stage_free_)
     if (e) cudaEventDestroy(e);
@@ -270,11 +276,25 @@ int Cache::Init(Tree* tree, int max_blocks) {
   if (cudaMalloc(&d_far_, (size_t)max_blocks_ * 8 * 4) != cudaSuccess) return fail(RAYT_E_OOM, "far pointer allocation failed");
   RAYT_CUDA_TRY(cudaMemsetAsync(d_far_, 0, (size_t)max_blocks_ * 8 * 4, stream_));
 
+  {
+    const char* io = std::getenv("RAYT_BLOCK_IO");
+    if (!(io && std::strcmp(io, "read") == 0)) file_host_ = tree->MapForDevice(&file_dev_);
+    if (!file_dev_) file_host_ = nullptr;
+    stats_.mapped = file_host_ ? 1 : 0;
+  }
   area_ = ((size_t)tree->info.content_bytes + 80 + 15) & ~(size_t)15;
-  stage_cap_ = (int)std::max<size_t>(kStageBlocksMin, kStageBytes / area_);
-  if (cudaHostAlloc(&h_stage_, area_ * stage_cap_ * 2, cudaHostAllocDefault) != cudaSuccess ||
-      cudaMalloc(&d_stage_, area_ * stage_cap_ * 2) != cudaSuccess ||
-      cudaHostAlloc(&h_slots_, sizeof(int) * stage_cap_ * 2, cudaHostAllocDefault) != cudaSuccess ||
+  if (file_host_) {
+    stage_cap_ = kMappedStageBlocks;
+    if (cudaHostAlloc(&h_blocks_, sizeof(int) * stage_cap_ * 2, cudaHostAllocDefault) != cudaSuccess ||
+        cudaMalloc(&d_blocks_, sizeof(int) * stage_cap_ * 2) != cudaSuccess)
+      return fail(RAYT_E_OOM, "staging allocation failed");
+  } else {
+    stage_cap_ = (int)std::max<size_t>(kStageBlocksMin, kStageBytes / area_);
+    if (cudaHostAlloc(&h_stage_, area_ * stage_cap_ * 2, cudaHostAllocDefault) != cudaSuccess ||
+        cudaMalloc(&d_stage_, area_ * stage_cap_ * 2) != cudaSuccess)
+      return fail(RAYT_E_OOM, "staging allocation failed");
+  }
+  if (cudaHostAlloc(&h_slots_, sizeof(int) * stage_cap_ * 2, cudaHostAllocDefault) != cudaSuccess ||
       cudaMalloc(&d_slots_, sizeof(int) * stage_cap_ * 2) != cudaSuccess)
     return fail(RAYT_E_OOM, "staging allocation failed");
   for (auto& e : stage_free_) RAYT_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -415,14 +435,23 @@ int Cache::FlushTo(int end) {
   if (end > batch_begin_) {
     const size_t first = (size_t)stage_cap_ * h + batch_begin_;
     const int n = end - batch_begin_;
-    uint8_t* hs = h_stage_ + area_ * first;
-    uint8_t* ds = d_stage_ + area_ * first;
-    RAYT_CUDA_TRY(cudaMemcpyAsync(ds, hs, area_ * n, cudaMemcpyHostToDevice, stream_));
+    UploadParams up{};
+    if (file_host_) {  // the kernel reads the blocks from the mapped file
+      RAYT_CUDA_TRY(cudaMemcpyAsync(d_blocks_ + first, h_blocks_ + first, sizeof(int) * n, cudaMemcpyHostToDevice,
+                                    stream_));
+      up.file = file_dev_;
+      up.file_first = tree_->info.header_bytes + 76;
+      up.file_stride = tree_->info.block_stride;
+      up.block_ids = d_blocks_ + first;
+    } else {
+      uint8_t* hs = h_stage_ + area_ * first;
+      uint8_t* ds = d_stage_ + area_ * first;
+      RAYT_CUDA_TRY(cudaMemcpyAsync(ds, hs, area_ * n, cudaMemcpyHostToDevice, stream_));
+      up.stage = ds + 80;
+      up.stride = area_;
+    }
     RAYT_CUDA_TRY(cudaMemcpyAsync(d_slots_ + first, h_slots_ + first, sizeof(int) * n, cudaMemcpyHostToDevice,
                                   stream_));
-    UploadParams up{};
-    up.stage = ds + 80;
-    up.stride = area_;
     up.slots = d_slots_ + first;
     up.blocks = n;
     up.nodes_in_block = nib_;
@@ -433,7 +462,7 @@ int Cache::FlushTo(int end) {
     }
     RAYT_CUDA_TRY(launch_upload(up, stream_));
     ++launches_;
-    stats_.bytes_h2d += (int64_t)(area_ * n);
+    stats_.bytes_h2d += (int64_t)(file_host_ ? (size_t)tree_->info.content_bytes * n : area_ * n);
   }
   size_t live = 0;  // patches newer content of their slot did not overwrite, in order
   for (size_t i = 0; i < patches_.size(); ++i)
@@ -517,23 +546,29 @@ int Cache::Unload() {
   return s;
 }
 
-// LoadBlock (stored-octree-loader.cpp:31-58) into staging position `pos` of
-// the current half, with the checks and the fault-link scan UploadBlock needs.
-// Safe to run on several threads for different positions.
+// LoadBlock (stored-octree-loader.cpp:31-58) for staging position `pos` of
+// the current half, with the checks and the fault-link scan UploadBlock needs:
+// the block record is read into the position's staging area, or, with the
+// file mapped, checked where it lies.  Safe to run on several threads for
+// different positions.
 int Cache::ReadOne(int pos, int block) {
   Staged& m = meta_[(size_t)stage_cap_ * half_ + pos];
   m.block = block;
   m.rc = RAYT_OK;
   m.faults.clear();
-  uint8_t* area = h_stage_ + area_ * ((size_t)stage_cap_ * half_ + pos);
-  const size_t content = tree_->info.content_bytes;
   const int64_t off = (int64_t)tree_->info.header_bytes + (int64_t)tree_->info.block_stride * (uint32_t)block;
-  if (!tree_->Read(off, 76 + content, area + 4)) {
-    m.rc = RAYT_E_IO;
-    m.err = "block read failed";
-    return m.rc;
+  const uint8_t* raw;  // the 76-byte block header, then the content (any alignment when mapped)
+  if (file_host_) {
+    raw = file_host_ + off;
+  } else {
+    uint8_t* area = h_stage_ + area_ * ((size_t)stage_cap_ * half_ + pos);
+    if (!tree_->Read(off, 76 + (size_t)tree_->info.content_bytes, area + 4)) {
+      m.rc = RAYT_E_IO;
+      m.err = "block read failed";
+      return m.rc;
+    }
+    raw = area + 4;
   }
-  const uint8_t* raw = area + 4;
   rayt_block_header& hdr = m.hdr;
   std::memcpy(&hdr.block_index, raw, 4);
   std::memcpy(&hdr.parent_block_index, raw + 4, 4);
@@ -559,19 +594,26 @@ int Cache::ReadOne(int pos, int block) {
         return bad("block root record is out of range");
     }
   }
-  const uint32_t* links = reinterpret_cast<const uint32_t*>(area + 80);
+  const uint8_t* links = raw + 76;
+  auto link = [links](int n) {
+    uint32_t l;
+    std::memcpy(&l, links + 4 * (size_t)n, 4);
+    return l;
+  };
   // Fault links name child blocks, most of them many times: keep each child
   // once, in order of first appearance (Place records a child under the first
   // link that names it, so later repeats change nothing there).
   ChildSet& seen = child_set();
   seen.Clear();
   if (validated_[block]) {  // links checked on an earlier load: only the fault children
-    for (int n = 0; n < nib_; ++n)
-      if ((links[n] & 255u) && ((links[n] >> 8) & 1u) && seen.Insert(links[n] >> 11)) m.faults.push_back(links[n] >> 11);
+    for (int n = 0; n < nib_; ++n) {
+      const uint32_t l = link(n);
+      if ((l & 255u) && ((l >> 8) & 1u) && seen.Insert(l >> 11)) m.faults.push_back(l >> 11);
+    }
     return RAYT_OK;
   }
   for (int n = 0; n < nib_; ++n) {
-    const uint32_t l = links[n], mask = l & 255u, ptr = l >> 11;
+    const uint32_t l = link(n), mask = l & 255u, ptr = l >> 11;
     if (!mask) continue;
     if (!((l >> 8) & 1u)) {
       // children inside the block: every one of them must be a node of the block
@@ -602,6 +644,7 @@ void Cache::StartRead(const int* blocks, int n) {
   read_started_ = std::chrono::steady_clock::now();
   for (int i = 0; i < n; ++i) {
     h_slots_[base + i] = -1;
+    if (h_blocks_) h_blocks_[base + i] = blocks[i];
     ready_[base + i].store(0, std::memory_order_relaxed);
   }
   pool_->Start(n, [this, first, base, blocks](int i) {

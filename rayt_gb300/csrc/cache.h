@@ -141,11 +141,21 @@ class Cache {
   std::vector<int> pending_;
   bool in_session_ = false, in_transaction_ = false;
 
-  // Block staging: two halves of stage_cap_ positions in pinned host memory
-  // and in device memory.  A position holds one block record read with a
-  // single pread: the 76-byte header at +4 and the content at +80, so the
-  // content is 16-byte aligned.  Positions [batch_begin_, staged_) of the
-  // current half form the batch the next flush uploads.
+  // Block staging: two halves of stage_cap_ positions.  Positions
+  // [batch_begin_, staged_) of the current half form the batch the next
+  // flush uploads.  Two ways to bring a block's bytes to the device:
+  // - mapped (the block file is mapped and registered with the device, see
+  //   Tree::MapForDevice): a position holds only the block's index; the reading
+  //   threads check the block where it lies in the page cache, and the upload
+  //   kernel reads its content from there;
+  // - read (the file cannot be mapped, or RAYT_BLOCK_IO=read): a position holds
+  //   one block record read with a single pread into pinned host memory - the
+  //   76-byte header at +4 and the content at +80, so the content is 16-byte
+  //   aligned - and a batch goes to the device in one copy.
+  const uint8_t* file_host_ = nullptr;  // mapped: the file in host memory
+  const uint8_t* file_dev_ = nullptr;   // mapped: the same bytes for kernels
+  int* h_blocks_ = nullptr;             // mapped: pinned, per position, the block index
+  int* d_blocks_ = nullptr;
   struct Staged {
     int block = -1;
     int rc = RAYT_OK;

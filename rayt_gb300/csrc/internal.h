@@ -200,6 +200,13 @@ struct UploadParams {
   int channels;
   int chan_bytes[kMaxChannels];
   uint8_t* chan[kMaxChannels]; // channel 0 = node links
+  // With `file` set, the contents are read where they lie in the mapped block
+  // file instead of from `stage`: block b's content starts at
+  // file + file_first + file_stride * block_ids[b], at any alignment.
+  const uint8_t* file;
+  uint64_t file_first;         // header bytes + the 76-byte block header
+  uint64_t file_stride;
+  const int* block_ids;
 };
 struct Patch {
   uint32_t index;  // node-link index (below 2^32) or far-pointer index

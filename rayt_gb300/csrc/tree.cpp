@@ -2,7 +2,10 @@
 //
 //  * rayt_tree_*: the reference's StoredOctreeLoader
 //    (rayt/CPU data/stored-octree-loader.cpp:9-98) over pread(2); the header
-//    layout is rayt/doc/storage data format.txt:1-33.
+//    layout is rayt/doc/storage data format.txt:1-33.  For the block cache the
+//    file can also be mapped and registered with the device once, so that
+//    streamed blocks are read by the upload kernel where they lie in the page
+//    cache instead of being copied into staging buffers first.
 //  * rayt_build_*: BuildOctree (rayt/CPU data/stored-octree-builder.h:40-41)
 //    through block_builder.h with the sources of scene_source.h.
 //  * rayt_camera_view_proj_inv: Camera::ViewProjectionMatrix().Inverse()
@@ -18,7 +21,10 @@
 #include <memory>
 #include <string>
 #include <vector>
+#include <cuda_runtime.h>
 #include <fcntl.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
 #include <unistd.h>
 
 #include "block_builder.h"
@@ -96,7 +102,44 @@ int Tree::LoadBlock(uint32_t index, rayt_block_header* hdr, void* content) const
   return RAYT_OK;
 }
 
+const uint8_t* Tree::MapForDevice(const uint8_t** device_map) {
+  std::lock_guard<std::mutex> lock(map_mu_);
+  if (!map_tried_) {
+    map_tried_ = true;
+    struct stat st {};
+    const uint64_t need = info.header_bytes + (uint64_t)info.block_stride * (info.blocks_count - 1) + 76 +
+                          info.content_bytes;  // the last block's record ends here
+    if (fd >= 0 && ::fstat(fd, &st) == 0 && (uint64_t)st.st_size >= need) {
+      const size_t page = (size_t)::sysconf(_SC_PAGESIZE);
+      const size_t len = ((size_t)st.st_size + page - 1) / page * page;
+      void* p = ::mmap(nullptr, len, PROT_READ, MAP_SHARED, fd, 0);
+      if (p != MAP_FAILED) {
+        map_ = static_cast<uint8_t*>(p);
+        map_len_ = len;
+        void* d = nullptr;
+        if (cudaHostRegister(map_, map_len_, cudaHostRegisterMapped | cudaHostRegisterPortable) == cudaSuccess) {
+          registered_ = true;
+          if (cudaHostGetDevicePointer(&d, map_, 0) == cudaSuccess) device_map_ = static_cast<const uint8_t*>(d);
+        }
+        cudaGetLastError();  // a refused registration leaves its error behind
+        if (!device_map_) {
+          if (registered_) cudaHostUnregister(map_);
+          registered_ = false;
+          ::munmap(map_, map_len_);
+          map_ = nullptr;
+        }
+      }
+    }
+  }
+  *device_map = device_map_;
+  return map_;
+}
+
 Tree::~Tree() {
+  if (map_) {
+    if (registered_) cudaHostUnregister(map_);
+    ::munmap(map_, map_len_);
+  }
   if (fd >= 0) ::close(fd);
 }
 

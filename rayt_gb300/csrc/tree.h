@@ -1,6 +1,7 @@
 // Block file reader (host).  See tree.cpp.
 #pragma once
 #include <cstdint>
+#include <mutex>
 #include <string>
 #include <vector>
 #include "../../include/rayt_gb300.h"
@@ -15,6 +16,21 @@ struct Tree {
   // header may be null; content (info.content_bytes) may be null
   int LoadBlock(uint32_t index, rayt_block_header* header, void* content) const;
   bool Read(int64_t off, size_t n, void* out) const;
+  // The whole file mapped read-only into host memory and registered with the
+  // device (page-locked, device-readable), made on first use and shared by
+  // every cache on this tree: a block's bytes are then at map + offset on the
+  // host and device_map + offset for kernels.  Null when the file cannot be
+  // mapped or registered, or is shorter than its header says; readers then use
+  // Read().
+  const uint8_t* MapForDevice(const uint8_t** device_map);
   ~Tree();
+
+ private:
+  std::mutex map_mu_;
+  bool map_tried_ = false;
+  uint8_t* map_ = nullptr;
+  size_t map_len_ = 0;
+  bool registered_ = false;
+  const uint8_t* device_map_ = nullptr;
 };
 }  // namespace rayt

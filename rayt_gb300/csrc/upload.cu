@@ -3,13 +3,15 @@
 // The reference rewrites each block's links on the CPU and issues one
 // clEnqueueWriteBuffer per channel plus one 4-byte write per parent pointer and
 // far pointer (rayt/GPU data/gpu-octree-cache.cpp:102-234,
-// gpu-octree-data.cpp:60-93).  Here a whole transaction's blocks arrive in one
-// host-to-device copy into a staging area; one kernel then scatters every block
-// into the channel buffers, rewriting stored links into the cache format on the
-// way (gpu-octree-cache.cpp:120-141: a loaded, non-fault link becomes a near
+// gpu-octree-data.cpp:60-93).  Here one kernel scatters a batch of blocks into
+// the channel buffers, rewriting stored links into the cache format on the way
+// (gpu-octree-cache.cpp:120-141: a loaded, non-fault link becomes a near
 // pointer relative to the node itself), and a second kernel applies the
 // parent/far-pointer writes, which the host has reduced to the last write per
-// address in the reference's order.
+// address in the reference's order.  The blocks come either from a staging
+// area filled by one host-to-device copy of the batch (upload_kernel) or
+// straight from the block file mapped into host memory and registered with the
+// device (upload_mapped_kernel: no host copy at all).
 #include "internal.h"
 
 namespace rayt {
@@ -55,6 +57,54 @@ __global__ void __launch_bounds__(kThreads) upload_kernel(const __grid_constant_
   }
 }
 
+// NearPointerValue rewrite of one stored link (see upload_kernel).
+__device__ __forceinline__ uint32_t cache_link(uint32_t l, uint32_t n) {
+  const uint32_t mask = l & 255u, fault = (l >> 8) & 1u;
+  if (mask && !fault) l = (((1u << 20) + (l >> 11) - n) << 11) | (l & (1u << 9)) | mask;
+  return l;
+}
+
+// One CTA per block, reading the block's content where it lies in the mapped
+// block file (host memory the device reads directly).  A block record starts
+// at any byte offset, so each warp reads 32 consecutive aligned words, every
+// lane its own, and forms the content words with a funnel shift from its word
+// and the next lane's (the warp's last lane reads its next word itself).  The
+// aligned words read hold at least one byte of the content (or of its block
+// header), so they lie inside the file.
+__global__ void __launch_bounds__(kThreads) upload_mapped_kernel(const __grid_constant__ UploadParams p) {
+  const int b = blockIdx.x;
+  if (p.slots[b] < 0) return;  // staged but not placed, or superseded
+  const size_t slot = (size_t)p.slots[b];
+  const size_t nib = (size_t)p.nodes_in_block;
+  const uint8_t* src = p.file + p.file_first + p.file_stride * (uint64_t)(uint32_t)p.block_ids[b];
+  const uint32_t mis = (uint32_t)(reinterpret_cast<uintptr_t>(src) & 3u);
+  const int lane = threadIdx.x & 31;
+  size_t off = 0;  // byte offset of the channel's section in the content
+  for (int c = 0; c < p.channels; ++c) {
+    const size_t bytes = nib * (size_t)p.chan_bytes[c];
+    uint8_t* d = p.chan[c] + slot * bytes;
+    if (((off | bytes) & 3u) == 0) {
+      const size_t words = bytes / 4, limit = words + (mis ? 1 : 0);
+      const uint32_t* a = reinterpret_cast<const uint32_t*>(src + off - mis);
+      uint32_t* d4 = reinterpret_cast<uint32_t*>(d);
+      for (size_t i0 = threadIdx.x & ~31u; i0 < words; i0 += kThreads) {  // warp-uniform trip count
+        const size_t i = i0 + lane;
+        const uint32_t lo = i < limit ? a[i] : 0u;
+        uint32_t w = lo;
+        if (mis) {
+          uint32_t hi = __shfl_down_sync(0xffffffffu, lo, 1);
+          if (lane == 31) hi = i + 1 < limit ? a[i + 1] : 0u;
+          w = __funnelshift_r(lo, hi, 8u * mis);
+        }
+        if (i < words) d4[i] = c == 0 ? cache_link(w, (uint32_t)i) : w;
+      }
+    } else {  // a section of odd size: bytes (links are always whole words)
+      for (size_t i = threadIdx.x; i < bytes; i += kThreads) d[i] = src[off + i];
+    }
+    off += bytes;
+  }
+}
+
 __global__ void patch_kernel(const Patch* patches, int n, uint32_t* links, uint32_t* far_ptrs) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -67,7 +117,8 @@ __global__ void patch_kernel(const Patch* patches, int n, uint32_t* links, uint3
 
 cudaError_t launch_upload(const UploadParams& p, cudaStream_t s) {
   if (p.blocks <= 0) return cudaSuccess;
-  upload_kernel<<<p.blocks, kThreads, 0, s>>>(p);
+  if (p.file) upload_mapped_kernel<<<p.blocks, kThreads, 0, s>>>(p);
+  else upload_kernel<<<p.blocks, kThreads, 0, s>>>(p);
   return cudaGetLastError();
 }
 
