@@ -66,11 +66,14 @@ __device__ __forceinline__ uint32_t cache_link(uint32_t l, uint32_t n) {
 
 // One CTA per block, reading the block's content where it lies in the mapped
 // block file (host memory the device reads directly).  A block record starts
-// at any byte offset, so each warp reads 32 consecutive aligned words, every
-// lane its own, and forms the content words with a funnel shift from its word
-// and the next lane's (the warp's last lane reads its next word itself).  The
-// aligned words read hold at least one byte of the content (or of its block
-// header), so they lie inside the file.
+// at any byte offset, so each warp reads rows of 32 consecutive aligned words,
+// every lane its own, and forms the content words with a funnel shift from its
+// word and the next lane's (the row's last lane takes the next row's first
+// word; after the last row it reads that word itself).  A warp issues four
+// rows' loads before it uses them, so that enough reads are in flight over
+// the host link.  The aligned words read hold at least one byte of the content
+// (or of its block header), so they lie inside the file.
+constexpr int kRows = 4;
 __global__ void __launch_bounds__(kThreads) upload_mapped_kernel(const __grid_constant__ UploadParams p) {
   const int b = blockIdx.x;
   if (p.slots[b] < 0) return;  // staged but not placed, or superseded
@@ -78,7 +81,7 @@ __global__ void __launch_bounds__(kThreads) upload_mapped_kernel(const __grid_co
   const size_t nib = (size_t)p.nodes_in_block;
   const uint8_t* src = p.file + p.file_first + p.file_stride * (uint64_t)(uint32_t)p.block_ids[b];
   const uint32_t mis = (uint32_t)(reinterpret_cast<uintptr_t>(src) & 3u);
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   size_t off = 0;  // byte offset of the channel's section in the content
   for (int c = 0; c < p.channels; ++c) {
     const size_t bytes = nib * (size_t)p.chan_bytes[c];
@@ -87,16 +90,28 @@ __global__ void __launch_bounds__(kThreads) upload_mapped_kernel(const __grid_co
       const size_t words = bytes / 4, limit = words + (mis ? 1 : 0);
       const uint32_t* a = reinterpret_cast<const uint32_t*>(src + off - mis);
       uint32_t* d4 = reinterpret_cast<uint32_t*>(d);
-      for (size_t i0 = threadIdx.x & ~31u; i0 < words; i0 += kThreads) {  // warp-uniform trip count
-        const size_t i = i0 + lane;
-        const uint32_t lo = i < limit ? a[i] : 0u;
-        uint32_t w = lo;
-        if (mis) {
-          uint32_t hi = __shfl_down_sync(0xffffffffu, lo, 1);
-          if (lane == 31) hi = i + 1 < limit ? a[i + 1] : 0u;
-          w = __funnelshift_r(lo, hi, 8u * mis);
+      // warp-uniform trip count: each warp takes 32 * kRows words at a time
+      for (size_t i0 = (size_t)warp * 32 * kRows; i0 < words; i0 += (size_t)kThreads * kRows) {
+        uint32_t lo[kRows];
+#pragma unroll
+        for (int r = 0; r < kRows; ++r) {
+          const size_t i = i0 + 32 * r + lane;
+          lo[r] = i < limit ? a[i] : 0u;
         }
-        if (i < words) d4[i] = c == 0 ? cache_link(w, (uint32_t)i) : w;
+        uint32_t after = 0u;  // the word after the last row, for its last lane
+        if (mis && lane == 31 && i0 + 32 * kRows < limit) after = a[i0 + 32 * kRows];
+#pragma unroll
+        for (int r = 0; r < kRows; ++r) {
+          uint32_t w = lo[r];
+          if (mis) {
+            uint32_t hi = __shfl_down_sync(0xffffffffu, lo[r], 1);
+            const uint32_t next_row = r + 1 < kRows ? __shfl_sync(0xffffffffu, lo[r + 1 < kRows ? r + 1 : r], 0) : after;
+            if (lane == 31) hi = next_row;
+            w = __funnelshift_r(lo[r], hi, 8u * mis);
+          }
+          const size_t i = i0 + 32 * r + lane;
+          if (i < words) d4[i] = c == 0 ? cache_link(w, (uint32_t)i) : w;
+        }
       }
     } else {  // a section of odd size: bytes (links are always whole words)
       for (size_t i = threadIdx.x; i < bytes; i += kThreads) d[i] = src[off + i];
