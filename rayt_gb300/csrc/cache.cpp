@@ -233,10 +233,7 @@ Cache::~Cache() {
   if (stream_) cudaStreamSynchronize(stream_);
   for (uint8_t* p : d_chan_) cudaFree(p);
   cudaFree(d_far_);
-  cudaFree(d_stage_);
-  cudaFree(d_slots_);
-  cudaFree(d_blocks_);
-  cudaFree(d_patches_);
+  cudaFree(d_stage_);  // d_slots_, d_blocks_, d_patches_ are the device views of the pinned arrays below
   cudaFreeHost(h_stage_);
   cudaFreeHost(h_slots_);
   cudaFreeHost(h_blocks_);
@@ -283,10 +280,17 @@ int Cache::Init(Tree* tree, int max_blocks) {
     stats_.mapped = file_host_ ? 1 : 0;
   }
   area_ = ((size_t)tree->info.content_bytes + 80 + 15) & ~(size_t)15;
+  // The per-position slot and block arrays and the patch records are small:
+  // they live in mapped pinned memory that the upload and patch kernels read
+  // directly (no copy per batch).
+  auto mapped_alloc = [](void** host, void** dev, size_t bytes) {
+    return cudaHostAlloc(host, bytes, cudaHostAllocMapped) == cudaSuccess &&
+           cudaHostGetDevicePointer(dev, *host, 0) == cudaSuccess;
+  };
   if (file_host_) {
     stage_cap_ = kMappedStageBlocks;
-    if (cudaHostAlloc(&h_blocks_, sizeof(int) * stage_cap_ * 2, cudaHostAllocDefault) != cudaSuccess ||
-        cudaMalloc(&d_blocks_, sizeof(int) * stage_cap_ * 2) != cudaSuccess)
+    if (!mapped_alloc(reinterpret_cast<void**>(&h_blocks_), reinterpret_cast<void**>(&d_blocks_),
+                      sizeof(int) * stage_cap_ * 2))
       return fail(RAYT_E_OOM, "staging allocation failed");
   } else {
     stage_cap_ = (int)std::max<size_t>(kStageBlocksMin, kStageBytes / area_);
@@ -294,8 +298,8 @@ int Cache::Init(Tree* tree, int max_blocks) {
         cudaMalloc(&d_stage_, area_ * stage_cap_ * 2) != cudaSuccess)
       return fail(RAYT_E_OOM, "staging allocation failed");
   }
-  if (cudaHostAlloc(&h_slots_, sizeof(int) * stage_cap_ * 2, cudaHostAllocDefault) != cudaSuccess ||
-      cudaMalloc(&d_slots_, sizeof(int) * stage_cap_ * 2) != cudaSuccess)
+  if (!mapped_alloc(reinterpret_cast<void**>(&h_slots_), reinterpret_cast<void**>(&d_slots_),
+                    sizeof(int) * stage_cap_ * 2))
     return fail(RAYT_E_OOM, "staging allocation failed");
   for (auto& e : stage_free_) RAYT_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   for (auto& e : patch_free_) RAYT_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -303,8 +307,8 @@ int Cache::Init(Tree* tree, int max_blocks) {
   ready_.reset(new std::atomic<uint8_t>[(size_t)stage_cap_ * 2]);
   for (size_t k = 0; k < (size_t)stage_cap_ * 2; ++k) ready_[k].store(0, std::memory_order_relaxed);
   patch_cap_ = stage_cap_ * 32 + 64;
-  if (cudaHostAlloc(&h_patches_, sizeof(Patch) * patch_cap_ * 2, cudaHostAllocDefault) != cudaSuccess ||
-      cudaMalloc(&d_patches_, sizeof(Patch) * patch_cap_ * 2) != cudaSuccess)
+  if (!mapped_alloc(reinterpret_cast<void**>(&h_patches_), reinterpret_cast<void**>(&d_patches_),
+                    sizeof(Patch) * patch_cap_ * 2))
     return fail(RAYT_E_OOM, "patch buffer allocation failed");
   {
     const char* e = std::getenv("RAYT_IO_THREADS");
@@ -437,8 +441,6 @@ int Cache::FlushTo(int end) {
     const int n = end - batch_begin_;
     UploadParams up{};
     if (file_host_) {  // the kernel reads the blocks from the mapped file
-      RAYT_CUDA_TRY(cudaMemcpyAsync(d_blocks_ + first, h_blocks_ + first, sizeof(int) * n, cudaMemcpyHostToDevice,
-                                    stream_));
       up.file = file_dev_;
       up.file_first = tree_->info.header_bytes + 76;
       up.file_stride = tree_->info.block_stride;
@@ -450,9 +452,7 @@ int Cache::FlushTo(int end) {
       up.stage = ds + 80;
       up.stride = area_;
     }
-    RAYT_CUDA_TRY(cudaMemcpyAsync(d_slots_ + first, h_slots_ + first, sizeof(int) * n, cudaMemcpyHostToDevice,
-                                  stream_));
-    up.slots = d_slots_ + first;
+    up.slots = d_slots_ + first;  // read by the kernel from pinned host memory
     up.blocks = n;
     up.nodes_in_block = nib_;
     up.channels = (int)d_chan_.size();
@@ -474,10 +474,9 @@ int Cache::FlushTo(int end) {
     const int ph = patch_half_;
     Patch* hp = h_patches_ + (size_t)patch_cap_ * ph;
     Patch* dp = d_patches_ + (size_t)patch_cap_ * ph;
-    // a pinned patch half is refilled only after its previous copy finished
+    // a pinned patch half is refilled only after the kernel that read it finished
     RAYT_CUDA_TRY(cudaEventSynchronize(patch_free_[ph]));
     std::memcpy(hp, patches_.data() + done, n * sizeof(Patch));
-    RAYT_CUDA_TRY(cudaMemcpyAsync(dp, hp, n * sizeof(Patch), cudaMemcpyHostToDevice, stream_));
     RAYT_CUDA_TRY(launch_patches(dp, (int)n, reinterpret_cast<uint32_t*>(d_chan_[0]), d_far_, stream_));
     RAYT_CUDA_TRY(cudaEventRecord(patch_free_[ph], stream_));
     patch_half_ ^= 1;
