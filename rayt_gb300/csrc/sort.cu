@@ -149,7 +149,7 @@ __device__ uint32_t warp_look_back(const unsigned long long* status, int tile, u
     const unsigned incl_mask = __ballot_sync(0xffffffffu, incl);
     const int first_nr = not_ready ? __ffs(not_ready) - 1 : 32;
     const int first_incl = incl_mask ? __ffs(incl_mask) - 1 : 32;
-    const int take = first_nr <= first_incl ? first_nr : first_incl + 1;  // lanes consumed this round
+    const int take = first_nr <= first_incl ? first_nr : first_incl + 1;  // lanes consumed by this read
     uint32_t v = lane < take && t >= 0 ? (uint32_t)w : 0u;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
