@@ -120,7 +120,9 @@ int rayt_build_terrain(const char* path, const rayt_terrain_params* params, int 
 typedef struct rayt_cache rayt_cache;
 
 /* GPUOctreeCacheManager(max_blocks_count, loader, context); max_blocks <= 0 means
- * every block of the file.  The tree must outlive the cache.  Renderers and
+ * every block of the file.  The cache keeps the tree open until the cache is
+ * destroyed (like the reference's shared loader), so rayt_tree_close may come
+ * first.  Renderers and
  * servers may share a cache (one LRU, one CUDA stream), one at a time: like
  * the reference's single-threaded frame loop, a cache is not used by two host
  * threads at once (a server's scheduler thread counts as one). */

@@ -14,9 +14,10 @@
 //     stored values (gpu-octree-cache.cpp:102-293).
 // What differs is the mechanics: the LRU is an intrusive doubly linked list
 // over slot ids with O(1) moves, block/parent lookups are flat arrays, and the
-// device side of a transaction is one pinned host->device copy of all its
-// blocks, one scatter kernel that rewrites links on the device, and one patch
-// kernel - instead of per-channel and per-pointer clEnqueueWriteBuffer calls.
+// device side of a batch of blocks is one scatter kernel that reads the blocks
+// from the block file mapped into host memory (or from one pinned staging
+// copy) and rewrites links on the device, and one patch kernel - instead of
+// per-channel and per-pointer clEnqueueWriteBuffer calls.
 #include "cache.h"
 
 #include <algorithm>
@@ -247,9 +248,11 @@ Cache::~Cache() {
     cudaEventDestroy(e.second);
   }
   if (stream_) cudaStreamDestroy(stream_);
+  Tree::Release(tree_);  // after every kernel that read its mapping has finished
 }
 
 int Cache::Init(Tree* tree, int max_blocks) {
+  tree->Retain();
   tree_ = tree;
   nib_ = (int)tree->info.nodes_in_block;
   max_blocks_ = max_blocks > 0 ? max_blocks : (int)tree->info.blocks_count;

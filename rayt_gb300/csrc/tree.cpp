@@ -272,7 +272,7 @@ int rayt_tree_open(const char* path, rayt_tree** out) {
   return RAYT_OK;
 }
 
-void rayt_tree_close(rayt_tree* tree) { delete reinterpret_cast<rayt::Tree*>(tree); }
+void rayt_tree_close(rayt_tree* tree) { rayt::Tree::Release(reinterpret_cast<rayt::Tree*>(tree)); }
 
 int rayt_tree_info_get(const rayt_tree* tree, rayt_tree_info* out) {
   if (!tree || !out) return fail(RAYT_E_ARG, "rayt_tree_info_get: null argument");

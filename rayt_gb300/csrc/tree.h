@@ -1,5 +1,6 @@
 // Block file reader (host).  See tree.cpp.
 #pragma once
+#include <atomic>
 #include <cstdint>
 #include <mutex>
 #include <string>
@@ -23,9 +24,16 @@ struct Tree {
   // mapped or registered, or is shorter than its header says; readers then use
   // Read().
   const uint8_t* MapForDevice(const uint8_t** device_map);
+  // The tree stays open while a cache uses it: rayt_tree_close and each cache
+  // on the tree hold one reference (a cache's kernels may read the mapping).
+  void Retain() { refs_.fetch_add(1); }
+  static void Release(Tree* t) {
+    if (t && t->refs_.fetch_sub(1) == 1) delete t;
+  }
   ~Tree();
 
  private:
+  std::atomic<int> refs_{1};
   std::mutex map_mu_;
   bool map_tried_ = false;
   uint8_t* map_ = nullptr;

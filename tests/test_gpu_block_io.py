@@ -75,6 +75,34 @@ def test_streamed_frames_identical_in_both_modes(trees):
             np.testing.assert_array_equal(a[2][k], b[2][k], err_msg="frame %d buffer %d" % (i, k))
 
 
+def test_tree_closed_before_its_cache(trees):
+    """Closing the tree while a cache still streams from its mapped file is
+    allowed: the cache keeps the tree open until it is destroyed.  Frames
+    streamed after the close equal frames with the tree left open."""
+    w, h = 160, 90
+    mats = [R.Camera(a, -30.0, 0.0, (0.5 - 0.6 * np.sin(np.radians(a)), 0.7, 0.5 + 0.6 * np.cos(np.radians(a))),
+                     60.0, w / h).view_proj_inv() for a in range(0, 360, 60)]
+    images = []
+    for close_early in (False, True):
+        ld, cm = _cache(trees["terrain8s"], 250, "mapped")
+        cm.InitialFillCache()
+        if close_early:
+            ld.close()
+        rt = R.GPURayTracer(cm, w, h)
+        rt.set_frame_time_limit(1e30)
+        rt.seed(3)
+        run = []
+        for m in mats:
+            rt.RenderFrame(m)
+            run.append(rt.read_image().copy())
+        assert cm.stats()["uploaded_blocks"] > 250
+        images.append(run)
+        rt.close()
+        cm.close()
+    for i, (a, b) in enumerate(zip(*images)):
+        np.testing.assert_array_equal(a, b, err_msg="frame %d" % i)
+
+
 def _write_tree(path, nib, extra_name, extra_bytes, rng):
     """A one-block tree: 'node links' (in-block child links and empty nodes)
     and one more channel; the channel name's length moves the block record's
