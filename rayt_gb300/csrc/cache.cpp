@@ -235,7 +235,6 @@ Cache::~Cache() {
   for (uint8_t* p : d_chan_) cudaFree(p);
   cudaFree(d_far_);
   cudaFree(d_stage_);  // d_slots_, d_blocks_, d_patches_ are the device views of the pinned arrays below
-  cudaFree(d_done_);
   cudaFreeHost(h_stage_);
   cudaFreeHost(h_slots_);
   cudaFreeHost(h_blocks_);
@@ -314,8 +313,6 @@ int Cache::Init(Tree* tree, int max_blocks) {
   if (!mapped_alloc(reinterpret_cast<void**>(&h_patches_), reinterpret_cast<void**>(&d_patches_),
                     sizeof(Patch) * patch_cap_ * 2))
     return fail(RAYT_E_OOM, "patch buffer allocation failed");
-  if (cudaMalloc(&d_done_, sizeof(unsigned)) != cudaSuccess) return fail(RAYT_E_OOM, "counter allocation failed");
-  RAYT_CUDA_TRY(cudaMemsetAsync(d_done_, 0, sizeof(unsigned), stream_));
   {
     const char* e = std::getenv("RAYT_IO_THREADS");
     int threads = e && std::atoi(e) > 0 ? std::atoi(e) : (int)std::thread::hardware_concurrency();
@@ -442,21 +439,6 @@ int Cache::FlushTo(int end) {
   }
   const std::pair<cudaEvent_t, cudaEvent_t> ev = flush_ev_[flush_used_++];
   RAYT_CUDA_TRY(cudaEventRecord(ev.first, stream_));
-  size_t live = 0;  // patches newer content of their slot did not overwrite, in order
-  for (size_t i = 0; i < patches_.size(); ++i)
-    if (!patch_dead_[i]) patches_[live++] = patches_[i];
-  patches_.resize(live);
-  // Copies a chunk of patches into the next pinned patch half (once the kernel
-  // that read that half before has finished) and returns its device view.
-  auto stage_patches = [this](size_t from, size_t n, Patch** dp) -> int {
-    const int ph = patch_half_;
-    RAYT_CUDA_TRY(cudaEventSynchronize(patch_free_[ph]));
-    std::memcpy(h_patches_ + (size_t)patch_cap_ * ph, patches_.data() + from, n * sizeof(Patch));
-    *dp = d_patches_ + (size_t)patch_cap_ * ph;
-    stats_.bytes_h2d += (int64_t)(n * sizeof(Patch));
-    return RAYT_OK;
-  };
-  size_t done = 0;
   if (end > batch_begin_) {
     const size_t first = (size_t)stage_cap_ * h + batch_begin_;
     const int n = end - batch_begin_;
@@ -481,35 +463,28 @@ int Cache::FlushTo(int end) {
       up.chan_bytes[c] = chan_bytes_[c];
       up.chan[c] = d_chan_[c];
     }
-    // the batch's first chunk of patches rides with the upload: its last CTA
-    // applies them after every block's content (no separate patch launch)
-    if (!patches_.empty()) {
-      done = std::min(patches_.size(), (size_t)patch_cap_);
-      Patch* dp = nullptr;
-      int rc = stage_patches(0, done, &dp);
-      if (rc != RAYT_OK) return rc;
-      up.patches = dp;
-      up.n_patches = (int)done;
-      up.far_ptrs = d_far_;
-      up.done = d_done_;
-    }
     RAYT_CUDA_TRY(launch_upload(up, stream_));
-    if (done) {
-      RAYT_CUDA_TRY(cudaEventRecord(patch_free_[patch_half_], stream_));
-      patch_half_ ^= 1;
-    }
     ++launches_;
     stats_.bytes_h2d += (int64_t)(file_host_ ? (size_t)tree_->info.content_bytes * n : area_ * n);
   }
-  while (done < patches_.size()) {  // patches without blocks, or beyond the first chunk
+  size_t live = 0;  // patches newer content of their slot did not overwrite, in order
+  for (size_t i = 0; i < patches_.size(); ++i)
+    if (!patch_dead_[i]) patches_[live++] = patches_[i];
+  patches_.resize(live);
+  size_t done = 0;
+  while (done < patches_.size()) {
     const size_t n = std::min(patches_.size() - done, (size_t)patch_cap_);
-    Patch* dp = nullptr;
-    int rc = stage_patches(done, n, &dp);
-    if (rc != RAYT_OK) return rc;
+    const int ph = patch_half_;
+    Patch* hp = h_patches_ + (size_t)patch_cap_ * ph;
+    Patch* dp = d_patches_ + (size_t)patch_cap_ * ph;
+    // a pinned patch half is refilled only after the kernel that read it finished
+    RAYT_CUDA_TRY(cudaEventSynchronize(patch_free_[ph]));
+    std::memcpy(hp, patches_.data() + done, n * sizeof(Patch));
     RAYT_CUDA_TRY(launch_patches(dp, (int)n, reinterpret_cast<uint32_t*>(d_chan_[0]), d_far_, stream_));
-    RAYT_CUDA_TRY(cudaEventRecord(patch_free_[patch_half_], stream_));
+    RAYT_CUDA_TRY(cudaEventRecord(patch_free_[ph], stream_));
     patch_half_ ^= 1;
     ++launches_;
+    stats_.bytes_h2d += (int64_t)(n * sizeof(Patch));
     done += n;
   }
   patches_.clear();

@@ -188,7 +188,6 @@ class Cache {
   Patch* d_patches_ = nullptr;
   int patch_cap_ = 0, patch_half_ = 0;
   cudaEvent_t patch_free_[2] = {nullptr, nullptr};
-  unsigned* d_done_ = nullptr;   // finished CTAs of an upload launch that carries patches
   std::vector<int> written_;     // per slot: batch epoch of its newest content
   std::vector<int> written_pos_; // per slot: staging index (both halves) of that content
   std::vector<int> patched_;     // per slot: batch epoch of its newest link patch

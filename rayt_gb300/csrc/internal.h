@@ -207,13 +207,6 @@ struct UploadParams {
   uint64_t file_first;         // header bytes + the 76-byte block header
   uint64_t file_stride;
   const int* block_ids;
-  // The batch's patches (n_patches > 0), applied by the CTA that finishes
-  // last, after every block's content is written; `done` counts finished CTAs
-  // (0 before the launch; the last CTA sets it back to 0).
-  const struct Patch* patches;
-  int n_patches;
-  uint32_t* far_ptrs;
-  unsigned* done;
 };
 struct Patch {
   uint32_t index;  // node-link index (below 2^32) or far-pointer index

@@ -19,29 +19,8 @@ namespace {
 
 constexpr int kThreads = 256;
 
-// The batch's patches, by the CTA that finishes the launch last: every CTA's
-// content writes are fenced before it counts itself done, so the last one
-// writes the patches after all contents (the sequential order's last writes).
-__device__ __forceinline__ void patches_after_contents(const UploadParams& p) {
-  if (p.n_patches <= 0) return;
-  __shared__ bool s_last;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) s_last = atomicAdd(p.done, 1u) == gridDim.x - 1;
-  __syncthreads();
-  if (!s_last) return;
-  __threadfence();
-  uint32_t* links = reinterpret_cast<uint32_t*>(p.chan[0]);
-  for (int i = threadIdx.x; i < p.n_patches; i += blockDim.x) {
-    const Patch q = p.patches[i];
-    if (q.far) p.far_ptrs[q.index] = q.value;
-    else links[q.index] = q.value;
-  }
-  if (threadIdx.x == 0) *p.done = 0u;  // for the next launch (stream order)
-}
-
 // One CTA per staged block: a grid-stride copy of each channel section.
-__device__ __forceinline__ void copy_staged_block(const UploadParams& p) {
+__global__ void __launch_bounds__(kThreads) upload_kernel(const __grid_constant__ UploadParams p) {
   const int b = blockIdx.x;
   const size_t nib = (size_t)p.nodes_in_block;
   const uint8_t* src = p.stage + (size_t)b * p.stride;
@@ -78,11 +57,6 @@ __device__ __forceinline__ void copy_staged_block(const UploadParams& p) {
   }
 }
 
-__global__ void __launch_bounds__(kThreads) upload_kernel(const __grid_constant__ UploadParams p) {
-  copy_staged_block(p);
-  patches_after_contents(p);
-}
-
 // NearPointerValue rewrite of one stored link (see upload_kernel).
 __device__ __forceinline__ uint32_t cache_link(uint32_t l, uint32_t n) {
   const uint32_t mask = l & 255u, fault = (l >> 8) & 1u;
@@ -100,7 +74,7 @@ __device__ __forceinline__ uint32_t cache_link(uint32_t l, uint32_t n) {
 // the host link.  The aligned words read hold at least one byte of the content
 // (or of its block header), so they lie inside the file.
 constexpr int kRows = 4;
-__device__ __forceinline__ void copy_mapped_block(const UploadParams& p) {
+__global__ void __launch_bounds__(kThreads) upload_mapped_kernel(const __grid_constant__ UploadParams p) {
   const int b = blockIdx.x;
   if (p.slots[b] < 0) return;  // staged but not placed, or superseded
   const size_t slot = (size_t)p.slots[b];
@@ -144,11 +118,6 @@ __device__ __forceinline__ void copy_mapped_block(const UploadParams& p) {
     }
     off += bytes;
   }
-}
-
-__global__ void __launch_bounds__(kThreads) upload_mapped_kernel(const __grid_constant__ UploadParams p) {
-  copy_mapped_block(p);
-  patches_after_contents(p);
 }
 
 __global__ void patch_kernel(const Patch* patches, int n, uint32_t* links, uint32_t* far_ptrs) {
