@@ -12,9 +12,10 @@ the frame workloads, and one compaction + radix sort + unique of the feedback
 words for c2.  Workloads (synthetic seeded scenes built by the block-file
 builder; no public dataset is involved):
   c1  depth-10 fBm heightfield (1024^3), 512x512, whole tree resident
-  c3  depth-12 heightfield + sphere shells (4096^3), 1920x1080 flythrough on
-      a seeded Catmull-Rom spline, block cache capped at 2 GiB, blocks
-      streamed from the file
+  c3  depth-12 heightfield + sphere shells (4096^3), 1920x1080 flythrough of
+      300 frames along a seeded Catmull-Rom spline (a shorter run times the
+      start of it at the same frame spacing), block cache capped at 2 GiB,
+      blocks streamed from the file
   c2  2^28 feedback words: 90% NO_HIT, Zipf(1.1) block IDs over 2^24
   c2r the same with block IDs over 2^28: the kept keys span more than 2^26
       values, so unique runs the LSD radix passes instead of the bitmap
@@ -50,6 +51,7 @@ sys.path.insert(0, ROOT)
 HBM_FALLBACK_GBS = 6800.0
 SCENE_DIR = os.environ.get("RAYT_SCENE_DIR", "/tmp/rayt_bench_scenes")
 C1_CAMERA = [45.0, -30.0, 0.0, -0.06, 0.66, 1.06, 60.0]
+C3_PATH_FRAMES = 300  # the C3 flythrough: 300 frames along one loop of the spline
 
 WORKLOADS = {
     "c1": {"depth": 10, "spheres": 0, "width": 512, "height": 512, "cache_bytes": 0, "lod": 1.0},
@@ -273,10 +275,12 @@ def scene_path(wl, local_rank, world):
     return path
 
 
-def camera_path(wl, frames, w, h, seed=3):
+def camera_path(wl, frames, w, h, seed=3, period=None):
     """C1: one fixed camera.  C3/C4: a Catmull-Rom spline through 8 control
     points drawn with `seed` inside the scene, looking along the path and 25 deg
-    down (C3 seed 3; C4 view v seed 7 + v)."""
+    down (C3 seed 3; C4 view v seed 7 + v).  Frame i sits at (i mod period) /
+    period of the closed loop; period defaults to `frames` (the whole loop in
+    the frames asked for)."""
     import rayt_gb300 as R
     if wl == "c1":
         c = R.Camera(C1_CAMERA[0], C1_CAMERA[1], C1_CAMERA[2], C1_CAMERA[3:6], C1_CAMERA[6], w / h)
@@ -295,8 +299,9 @@ def camera_path(wl, frames, w, h, seed=3):
 
     out = []
     span = len(pts) - 3
+    period = max(1, period or frames)
     for i in range(frames):
-        u = span * i / max(1, frames)
+        u = span * (i % period) / period
         p = spline(u)
         q = spline(min(span - 1e-3, u + 0.01))
         d = q - p
@@ -418,7 +423,10 @@ def bench_frames(args, rank, world, local):
     w, h = cfg["width"], cfg["height"]
     steps = args.steps or (300 if wl == "c3" else 200)
     path = scene_path(wl, local, world)
-    mats = camera_path(wl, args.warmup + steps, w, h)
+    # C3 is 300 frames along its spline: whatever the number of frames run,
+    # they sit at that spacing (a short run covers the start of the flythrough
+    # at the configured camera speed, not the whole loop at a higher one)
+    mats = camera_path(wl, args.warmup + steps, w, h, period=C3_PATH_FRAMES if wl == "c3" else None)
     threads = os.cpu_count() or 1
 
     if args.impl == "reference":
