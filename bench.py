@@ -468,6 +468,7 @@ def bench_frames(args, rank, world, local):
     barrier(world)
     clocks = ClockSampler(local)
     clocks.start()
+    cs0 = cm.stats()
     ms_dev, wall = 0.0, 0.0
     passes, launches, h2d, d2h, uploaded, trace_ms = 0, 0, 0, 0, 0, 0.0
     part_ms = {k: 0.0 for k in ("gpu_ms_feedback", "gpu_ms_upload", "host_ms_wait", "host_ms_decode", "host_ms_load")}
@@ -502,10 +503,20 @@ def bench_frames(args, rank, world, local):
     torch.cuda.synchronize()
     barrier(world)
     clk = clocks.stop()
+    cs1 = cm.stats()
     t_dev = max_over_ranks(ms_dev / 1e3, world)
     t_wall = max_over_ranks(wall, world)
     rays = float(w * h * steps)
     total_rays = sum_over_ranks(rays, world)
+    # block streaming over the timed frames: block content and patches moved
+    # to the device, bytes of the block file read, and the rate the upload
+    # launches moved them at (their device time)
+    up_ms = part_ms["gpu_ms_upload"]
+    streaming = {"h2d_bytes_per_frame": int(h2d / steps),
+                 "file_bytes_per_frame": int((cs1["bytes_read"] - cs0["bytes_read"]) / steps),
+                 "upload_gbs": round(h2d / (up_ms / 1e3) / 1e9, 1) if up_ms > 0 else None,
+                 "block_source": "block file mapped into host memory, read by the upload kernel"
+                                 if cs1["mapped"] else "pread into pinned staging, one copy per batch"}
 
     # roofline of the dominant kernel (first-pass traversal) on the last camera
     m_last = mats[args.warmup + steps - 1]
@@ -546,6 +557,7 @@ def bench_frames(args, rank, world, local):
         "frames": {"passes_per_frame": round(passes / steps, 3), "uploaded_blocks_per_frame": round(uploaded / steps, 2),
                    "trace_ms_per_frame": round(trace_ms / steps, 4),
                    **{k.replace("_ms_", "_") + "_ms_per_frame": round(v / steps, 4) for k, v in part_ms.items()}},
+        "streaming": streaming,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "traffic_rule": traffic_rule,
                      "peak_source": peak_kind,

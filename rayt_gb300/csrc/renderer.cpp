@@ -102,7 +102,7 @@ class Renderer {
   int Trace(int it, bool count, int rays);
   UniqueFromBitsParams UniqueParams(int it) const;
   int RunPass(int it, int rays, int* launches);
-  int PassGraph(int kind, int it);
+  int PassGraph(int kind, int it, int rays);
   int groups() const { return (int)group_tiles_.size(); }
 
   // One pass's device work (clear feedback state, traversal, unique) as a
@@ -115,6 +115,7 @@ class Renderer {
     std::vector<cudaGraphNode_t> trace_nodes;
     TraceParams key;  // the parameters (without views) it was built with
     int ctas = 0;     // and the persistent kernel's CTAs per SM
+    unsigned blocks = 0;  // later passes: the traversal node's grid now
   };
   Graph graphs_[3];
   void DropGraphs();
@@ -341,7 +342,7 @@ UniqueFromBitsParams Renderer::UniqueParams(int it) const {
 // Builds (when missing or when the pass parameters changed) and updates the
 // graph of pass kind `kind`, then launches it.  Events 1 (after traversal)
 // and 2 (after unique) are recorded inside the graph.
-int Renderer::PassGraph(int kind, int it) {
+int Renderer::PassGraph(int kind, int it, int rays) {
   Graph& g = graphs_[kind];
   TraceParams key = Params(it);
   if (g.exec && (std::memcmp(&key, &g.key, sizeof(key)) != 0 || g.ctas != ctas_per_sm)) {
@@ -380,7 +381,8 @@ int Renderer::PassGraph(int kind, int it) {
     cudaError_t e = cudaGraphAddMemsetNode(&node, graph, nullptr, 0, &mp);
     prev = node;
     for (size_t i = 0; e == cudaSuccess && i < tp.size(); ++i) {
-      trace_node_params(&tp[i], first, false, first ? group_tiles_[i] * 32 : 0, grid, args, &kp);
+      trace_node_params(&tp[i], first, false, first ? group_tiles_[i] * 32 : rays, grid, args, &kp);
+      g.blocks = kp.gridDim.x;
       e = cudaGraphAddKernelNode(&node, graph, &prev, 1, &kp);
       g.trace_nodes.push_back(node);
       prev = node;
@@ -409,6 +411,13 @@ int Renderer::PassGraph(int kind, int it) {
       trace_node_params(&tp[i], true, false, group_tiles_[i] * 32, grid, args, &kp);
       RAYT_CUDA_TRY(cudaGraphExecKernelNodeSetParams(g.exec, g.trace_nodes[i], &kp));
     }
+  } else {
+    // a later pass's grid follows its ray count
+    trace_node_params(&tp[0], false, false, rays, grid, args, &kp);
+    if (kp.gridDim.x != g.blocks) {
+      RAYT_CUDA_TRY(cudaGraphExecKernelNodeSetParams(g.exec, g.trace_nodes[0], &kp));
+      g.blocks = kp.gridDim.x;
+    }
   }
   RAYT_CUDA_TRY(cudaGraphLaunch(g.exec, s_));
   return RAYT_OK;
@@ -419,7 +428,7 @@ int Renderer::PassGraph(int kind, int it) {
 int Renderer::RunPass(int it, int rays, int* launches) {
   RAYT_CUDA_TRY(cudaEventRecord(ev_[0], s_));
   if (use_graphs && !record) {
-    int rc = PassGraph(it == 0 ? 0 : ((it & 1) ? 1 : 2), it);
+    int rc = PassGraph(it == 0 ? 0 : ((it & 1) ? 1 : 2), it, rays);
     if (rc != RAYT_OK) return rc;
     *launches += (it == 0 ? groups() : 1) + 1;
     return RAYT_OK;

@@ -33,6 +33,8 @@
 // FP32 arithmetic follows the reference's operation order exactly; the file is
 // compiled with --fmad=false and IEEE division/sqrt so no operation is fused or
 // approximated, which keeps hit node IDs identical to the CPU oracle.
+#include <algorithm>
+
 #include "internal.h"
 
 namespace rayt {
@@ -920,8 +922,13 @@ int queue_grid() {
 template <bool kFirst, bool kCount>
 void trace_launch_shape(const TraceParams& p, int rays, int grid, void** func, dim3* blocks) {
   if (!kFirst) {
+    // persistent warps over the faulted rays; when the caller knows their
+    // count, no more CTAs than they fill (a later pass often traces a few
+    // hundred rays, and every idle warp of a full grid still launches and
+    // claims from the one work counter)
     *func = reinterpret_cast<void*>(trace_queue_kernel<false, kCount>);
-    *blocks = dim3(queue_grid<kCount>());
+    const int full = queue_grid<kCount>();
+    *blocks = dim3(rays > 0 ? std::min(full, (rays + kBlockThreads - 1) / kBlockThreads) : full);
   } else if (p.refill < 32) {
     *func = reinterpret_cast<void*>(trace_persistent_kernel<true, kCount>);
     *blocks = dim3(grid > 0 ? grid : persistent_grid<true, kCount>());
