@@ -822,6 +822,54 @@ int Cache::MarkParentUsed(int slot) {
   else Touch(p);
   return RAYT_OK;
 }
+// The feedback's marks of one pass: MarkBlockAsUsed for each hit block, then
+// MarkParentAsUsed for each duplicate hit (ray-tracing-feedback-extractor.cpp
+// order), with the list ending exactly as after the calls one by one.  One
+// by one, every call moves its block and each ancestor up to the root block
+// to the MRU end, so the list ends with the untouched slots in their old
+// order followed by every touched slot in the order of its last move; and a
+// marker reaches the front (and is taken off) once every slot before it has
+// moved, which the last call's DequeueMarkers sees too, since nothing is
+// inserted ahead of a marker.  The last move of a slot falls in the last call
+// whose chain holds it, at its place in that chain (below its ancestors).
+// Walking the calls from the last back, a chain stops at the first slot
+// already seen (every ancestor of it was seen with it), so the batch walks
+// each touched slot once instead of every chain to the root block (a pass
+// marks up to 4000 blocks, most of them sharing their upper ancestors).
+void Cache::MarkUsedBatch(const std::vector<int>& hits, const std::vector<int>& dup_hits) {
+  touch_starts_.clear();
+  for (int s : hits)
+    if (s >= 0 && s < first_free_) touch_starts_.push_back(s);
+  bool any = !touch_starts_.empty();
+  for (int s : dup_hits) {
+    if (s < 0 || s >= first_free_) continue;
+    any = true;  // a root-level parent only dequeues markers
+    if (slots_[s].parent != (int)kRootParent) touch_starts_.push_back(slots_[s].parent);
+  }
+  if (!any) return;
+  if (touch_seen_.size() != (size_t)max_blocks_) touch_seen_.assign(max_blocks_, 0u);
+  if (++touch_epoch_ == 0) {
+    std::fill(touch_seen_.begin(), touch_seen_.end(), 0u);
+    touch_epoch_ = 1;
+  }
+  touch_order_.clear();
+  touch_groups_.clear();
+  for (size_t i = touch_starts_.size(); i-- > 0;) {
+    const int begin = (int)touch_order_.size();
+    for (int s = touch_starts_[i]; s != (int)kRootParent && touch_seen_[s] != touch_epoch_; s = slots_[s].parent) {
+      touch_seen_[s] = touch_epoch_;
+      touch_order_.push_back(s);
+    }
+    if ((int)touch_order_.size() > begin) touch_groups_.emplace_back(begin, (int)touch_order_.size());
+  }
+  for (size_t g = touch_groups_.size(); g-- > 0;)
+    for (int k = touch_groups_[g].first; k < touch_groups_[g].second; ++k) {
+      Unlink(touch_order_[k]);
+      InsertBefore(touch_order_[k], head_);
+    }
+  DequeueMarkers();
+}
+
 // RequestBlock (gpu-octree-cache-manager.cpp:138-148)
 int Cache::RequestBlock(int block) {
   if (!in_transaction_) return fail(RAYT_E_STATE, "request outside a transaction");

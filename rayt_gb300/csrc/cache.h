@@ -81,6 +81,10 @@ class Cache {
   int StartTransaction();
   int MarkBlockUsed(int slot);
   int MarkParentUsed(int slot);
+  // MarkBlockUsed for every slot of hits, then MarkParentUsed for every slot
+  // of dup_hits, in that order, applied as one batch with the same result
+  // (slots out of range are skipped, as the one-by-one calls refuse them).
+  void MarkUsedBatch(const std::vector<int>& hits, const std::vector<int>& dup_hits);
   int RequestBlock(int block);
   bool TransactionFilled() const { return markers_[kTransaction].hit; }
   bool SessionFilled() const { return markers_[kSession].hit; }
@@ -201,6 +205,13 @@ class Cache {
   static constexpr int kFlushEvents = 256;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> flush_ev_;  // per flushed batch, reused
   int flush_used_ = 0;
+
+  // MarkUsedBatch's scratch: chain starts in call order, the nodes whose last
+  // move falls in each call (walk order), those calls' ranges, seen stamps
+  std::vector<int> touch_starts_, touch_order_;
+  std::vector<std::pair<int, int>> touch_groups_;
+  std::vector<uint32_t> touch_seen_;
+  uint32_t touch_epoch_ = 0;
 
   // list helpers
   void Unlink(int id);

@@ -500,8 +500,7 @@ int Renderer::Frame(const float* m) {
     const auto td = clock::now();
     fb_.Decode(h_unique_, h_counts_[0], rand);
     if ((rc = cache_->StartTransaction()) != RAYT_OK) break;
-    for (int b2 : fb_.hits) cache_->MarkBlockUsed(b2);
-    for (int b2 : fb_.dup_hits) cache_->MarkParentUsed(b2);
+    cache_->MarkUsedBatch(fb_.hits, fb_.dup_hits);
     for (int f : fb_.faults) {
       if (cache_->TransactionFilled()) break;
       if ((rc = cache_->RequestBlock(f)) != RAYT_OK) break;

@@ -428,8 +428,7 @@ int Server::Step(int* finished) {
   int rc = cache_->StartSession();
   if (rc == RAYT_OK) rc = cache_->StartTransaction();
   if (rc == RAYT_OK) {
-    for (int b : fb_.hits) cache_->MarkBlockUsed(b);
-    for (int b : fb_.dup_hits) cache_->MarkParentUsed(b);
+    cache_->MarkUsedBatch(fb_.hits, fb_.dup_hits);
     for (int b : fb_.faults) {
       if (cache_->TransactionFilled()) break;
       if ((rc = cache_->RequestBlock(b)) != RAYT_OK) break;
