@@ -207,6 +207,7 @@ struct UploadParams {
   uint64_t file_first;         // header bytes + the 76-byte block header
   uint64_t file_stride;
   const int* block_ids;
+  int parts;                   // CTAs per block (mapped reads; set by launch_upload)
 };
 struct Patch {
   uint32_t index;  // node-link index (below 2^32) or far-pointer index

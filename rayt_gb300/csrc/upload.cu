@@ -12,6 +12,8 @@
 // area filled by one host-to-device copy of the batch (upload_kernel) or
 // straight from the block file mapped into host memory and registered with the
 // device (upload_mapped_kernel: no host copy at all).
+#include <algorithm>
+
 #include "internal.h"
 
 namespace rayt {
@@ -64,8 +66,13 @@ __device__ __forceinline__ uint32_t cache_link(uint32_t l, uint32_t n) {
   return l;
 }
 
-// One CTA per block, reading the block's content where it lies in the mapped
-// block file (host memory the device reads directly).  A block record starts
+// `parts` CTAs per block, each a contiguous share of every channel section,
+// reading the block's content where it lies in the mapped block file (host
+// memory the device reads directly).  A read over the host link takes long
+// enough that a CTA copies a block's share in a few rounds of loads; a small
+// batch (a transaction of a later pass streams a few dozen blocks) spreads
+// each block over several CTAs so that more SMs have reads in flight.  A block
+// record starts
 // at any byte offset, so each warp reads rows of 32 consecutive aligned words,
 // every lane its own, and forms the content words with a funnel shift from its
 // word and the next lane's (the row's last lane takes the next row's first
@@ -75,7 +82,7 @@ __device__ __forceinline__ uint32_t cache_link(uint32_t l, uint32_t n) {
 // (or of its block header), so they lie inside the file.
 constexpr int kRows = 4;
 __global__ void __launch_bounds__(kThreads) upload_mapped_kernel(const __grid_constant__ UploadParams p) {
-  const int b = blockIdx.x;
+  const int b = blockIdx.x / p.parts, part = blockIdx.x - b * p.parts;
   if (p.slots[b] < 0) return;  // staged but not placed, or superseded
   const size_t slot = (size_t)p.slots[b];
   const size_t nib = (size_t)p.nodes_in_block;
@@ -90,8 +97,12 @@ __global__ void __launch_bounds__(kThreads) upload_mapped_kernel(const __grid_co
       const size_t words = bytes / 4, limit = words + (mis ? 1 : 0);
       const uint32_t* a = reinterpret_cast<const uint32_t*>(src + off - mis);
       uint32_t* d4 = reinterpret_cast<uint32_t*>(d);
+      // this CTA's words [w0, w1); loads past w1 stay below limit (inside the
+      // section, or its one trailing word) and are not stored
+      const size_t per = (words + p.parts - 1) / p.parts;
+      const size_t w0 = min(words, per * part), w1 = min(words, w0 + per);
       // warp-uniform trip count: each warp takes 32 * kRows words at a time
-      for (size_t i0 = (size_t)warp * 32 * kRows; i0 < words; i0 += (size_t)kThreads * kRows) {
+      for (size_t i0 = w0 + (size_t)warp * 32 * kRows; i0 < w1; i0 += (size_t)kThreads * kRows) {
         uint32_t lo[kRows];
 #pragma unroll
         for (int r = 0; r < kRows; ++r) {
@@ -110,11 +121,13 @@ __global__ void __launch_bounds__(kThreads) upload_mapped_kernel(const __grid_co
             w = __funnelshift_r(lo[r], hi, 8u * mis);
           }
           const size_t i = i0 + 32 * r + lane;
-          if (i < words) d4[i] = c == 0 ? cache_link(w, (uint32_t)i) : w;
+          if (i < w1) d4[i] = c == 0 ? cache_link(w, (uint32_t)i) : w;
         }
       }
     } else {  // a section of odd size: bytes (links are always whole words)
-      for (size_t i = threadIdx.x; i < bytes; i += kThreads) d[i] = src[off + i];
+      const size_t per = (bytes + p.parts - 1) / p.parts;
+      const size_t b0 = min(bytes, per * part), b1 = min(bytes, b0 + per);
+      for (size_t i = b0 + threadIdx.x; i < b1; i += kThreads) d[i] = src[off + i];
     }
     off += bytes;
   }
@@ -132,8 +145,20 @@ __global__ void patch_kernel(const Patch* patches, int n, uint32_t* links, uint3
 
 cudaError_t launch_upload(const UploadParams& p, cudaStream_t s) {
   if (p.blocks <= 0) return cudaSuccess;
-  if (p.file) upload_mapped_kernel<<<p.blocks, kThreads, 0, s>>>(p);
-  else upload_kernel<<<p.blocks, kThreads, 0, s>>>(p);
+  if (p.file) {
+    // about two CTAs per SM over the batch, at most 8 per block
+    static const int sms = [] {
+      int dev = 0, n = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+      return n > 0 ? n : 1;
+    }();
+    UploadParams q = p;
+    q.parts = std::max(1, std::min(8, (2 * sms + p.blocks - 1) / p.blocks));
+    upload_mapped_kernel<<<(unsigned)(p.blocks * q.parts), kThreads, 0, s>>>(q);
+  } else {
+    upload_kernel<<<p.blocks, kThreads, 0, s>>>(p);
+  }
   return cudaGetLastError();
 }
 
