@@ -428,6 +428,14 @@ int rayt_selftest_bounded_wait(double limit_s, void* stream);
  * happen within a few calls. */
 int rayt_testing_set_lookback_epoch(uint32_t calls);
 
+/* No counterpart in the reference.  Testing hook for the renderer's feedback
+ * marks: rayt_cache_mark_block_used for every slot of hits, then
+ * rayt_cache_mark_parent_used for every slot of dup_hits, applied the way a
+ * frame applies a pass's marks (one batch that leaves the LRU list and the
+ * session/transaction markers as the calls one by one would; slots out of
+ * range are skipped, as those calls refuse them).  Needs an open transaction. */
+int rayt_testing_cache_mark_batch(rayt_cache* cache, const int* hits, int n_hits, const int* dup_hits, int n_dup);
+
 #ifdef __cplusplus
 }
 #endif

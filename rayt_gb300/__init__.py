@@ -162,6 +162,7 @@ def lib():
         "rayt_cache_depth_view": (i32, [vp, C.POINTER(f32), f32, i32, i32, vp, vp]),
         "rayt_selftest_bounded_wait": (i32, [C.c_double, vp]),
         "rayt_testing_set_lookback_epoch": (i32, [u32]),
+        "rayt_testing_cache_mark_batch": (i32, [vp, C.POINTER(i32), i32, C.POINTER(i32), i32]),
         "rayt_server_create": (i32, [vp, C.POINTER(ServerConfig), C.POINTER(vp)]),
         "rayt_server_destroy": (None, [vp]),
         "rayt_server_add_client": (i32, [vp, i32, i32, C.POINTER(i32)]),

@@ -314,14 +314,17 @@ int Cache::Init(Tree* tree, int max_blocks) {
                     sizeof(Patch) * patch_cap_ * 2))
     return fail(RAYT_E_OOM, "patch buffer allocation failed");
   {
-    // Block checks on the mapped file are cheap (about 1.6 us a block), and
-    // the pool's workers spin from StartTransaction until the reads arrive,
-    // where they compete with the decode and LRU marks on the calling thread:
-    // 8 threads beat 16 by 6% per c3 frame (4, 6 and 12 fell between).  Reads
-    // with pread into staging take 16.
+    // Block checks on the mapped file are cheap (about 1.6 us for 4096
+    // links), and the pool's workers spin from StartTransaction until the
+    // reads arrive, where they compete with the decode and LRU marks on the
+    // calling thread: for blocks of up to 4096 nodes 8 threads beat 16 by 6%
+    // per c3 frame (4, 6 and 12 fell between).  Larger blocks (the served
+    // workload's 16384 nodes) take 4x the check each and keep 16, as do reads
+    // with pread into staging.
     const char* e = std::getenv("RAYT_IO_THREADS");
     const int hw = std::max(1, (int)std::thread::hardware_concurrency());
-    int threads = e && std::atoi(e) > 0 ? std::atoi(e) : std::min(hw, file_host_ ? 8 : 16);
+    const int want = file_host_ && nib_ <= 4096 ? 8 : 16;
+    int threads = e && std::atoi(e) > 0 ? std::atoi(e) : std::min(hw, want);
     threads = std::max(1, std::min(threads, 16));
     pool_ = new ReadPool(threads - 1);  // the calling thread reads too
   }
@@ -1007,6 +1010,14 @@ int rayt_cache_mark_parent_used(rayt_cache* c, int slot) {
   if (!c) return fail(RAYT_E_ARG, "null cache");
   if (!C(c)->in_transaction()) return fail(RAYT_E_STATE, "mark outside a transaction");
   return C(c)->MarkParentUsed(slot);
+}
+int rayt_testing_cache_mark_batch(rayt_cache* c, const int* hits, int n_hits, const int* dup_hits, int n_dup) {
+  if (!c || n_hits < 0 || n_dup < 0 || (n_hits > 0 && !hits) || (n_dup > 0 && !dup_hits))
+    return fail(RAYT_E_ARG, "rayt_testing_cache_mark_batch: bad argument");
+  if (!C(c)->in_transaction()) return fail(RAYT_E_STATE, "mark outside a transaction");
+  const std::vector<int> h(hits, hits + n_hits), d(dup_hits, dup_hits + n_dup);
+  C(c)->MarkUsedBatch(h, d);
+  return RAYT_OK;
 }
 int rayt_cache_request_block(rayt_cache* c, int block) { return c ? C(c)->RequestBlock(block) : fail(RAYT_E_ARG, "null cache"); }
 int rayt_cache_transaction_filled(const rayt_cache* c, int* out) {
