@@ -449,28 +449,40 @@ def bench_frames(args, rank, world, local):
 
     torch.cuda.set_device(local)
     ld = R.StoredOctreeLoader(path)
-    cm = R.GPUOctreeCacheManager(cache_blocks(cfg), ld)
-    t0 = time.time()
-    cm.InitialFillCache()
-    fill_s = time.time() - t0
-    rt = R.GPURayTracer(cm, w, h)
-    rt.set_lod_voxel_size(cfg["lod"])
-    rt.set_frame_time_limit(1e30)
-    rt.seed(1)  # the hit-window generator; the parity check replays the same sequence
-    stream = torch.cuda.ExternalStream(rt.stream_handle())
+
+    def renderer(host_image=None):
+        """A fresh cache (InitialFillCache) and renderer that have rendered the
+        warm-up frames; host_image: deliver every frame there."""
+        c = R.GPUOctreeCacheManager(cache_blocks(cfg), ld)
+        t0 = time.time()
+        c.InitialFillCache()
+        fill = time.time() - t0
+        r = R.GPURayTracer(c, w, h)
+        r.set_lod_voxel_size(cfg["lod"])
+        r.set_frame_time_limit(1e30)
+        r.seed(1)  # the hit-window generator; the parity check replays the same sequence
+        if host_image is not None:
+            r.set_host_image(host_image.data_ptr(), host_image.numel())
+        for i in range(args.warmup):
+            r.RenderFrame(mats[i])
+        return c, r, fill
+
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > L2 (129 MB)
-    pinned = torch.empty((h, w, 4), dtype=torch.uint8).pin_memory()
     timed_imgs = []  # the first parity_frames timed images, checked against the oracle afterwards
 
-    for i in range(args.warmup):
-        rt.RenderFrame(mats[i])
+    # device-timed frames (value): each frame's image stays in device memory;
+    # the wall clock around RenderFrame plus a read-back of the image after
+    # the call is reported beside the end-to-end number (e2e_read_after)
+    pinned_after = torch.empty((h, w, 4), dtype=torch.uint8).pin_memory()
+    cm, rt, fill_s = renderer()
+    stream = torch.cuda.ExternalStream(rt.stream_handle())
     torch.cuda.synchronize()
     barrier(world)
     clocks = ClockSampler(local)
     clocks.start()
     cs0 = cm.stats()
-    ms_dev, wall = 0.0, 0.0
-    passes, launches, h2d, d2h, uploaded, trace_ms = 0, 0, 0, 0, 0, 0.0
+    ms_dev, wall_after = 0.0, 0.0
+    passes, launches, h2d, uploaded, trace_ms = 0, 0, 0, 0, 0.0
     part_ms = {k: 0.0 for k in ("gpu_ms_feedback", "gpu_ms_upload", "host_ms_wait", "host_ms_decode", "host_ms_load")}
     lat = []
     for i in range(args.warmup, args.warmup + steps):
@@ -482,11 +494,8 @@ def bench_frames(args, rank, world, local):
         e0.record(stream)
         rt.RenderFrame(mats[i])
         e1.record(stream)
-        # end to end: the frame's RGBA8 image read back to pinned host memory
-        R._check(R.lib().rayt_renderer_read_image(rt._h, pinned.data_ptr(), pinned.numel()))
-        wall += time.perf_counter() - t
-        if len(timed_imgs) < args.parity_frames:
-            timed_imgs.append(pinned.numpy().copy())
+        R._check(R.lib().rayt_renderer_read_image(rt._h, pinned_after.data_ptr(), pinned_after.numel()))
+        wall_after += time.perf_counter() - t
         e1.synchronize()
         d = e0.elapsed_time(e1)
         ms_dev += d
@@ -495,17 +504,49 @@ def bench_frames(args, rank, world, local):
         passes += st["passes"]
         launches += st["kernel_launches"]
         h2d += st["bytes_h2d"]
-        d2h += st["bytes_d2h"] + w * h * 4
         uploaded += st["uploaded_blocks"]
         trace_ms += st["gpu_ms_trace"]
         for k in part_ms:
             part_ms[k] += st[k]
     torch.cuda.synchronize()
+    cs1 = cm.stats()
+    n_cache_blocks = cm.blocks()[1]
+
+    # roofline of the dominant kernel (first-pass traversal) on the last camera
+    m_last = mats[args.warmup + steps - 1]
+    fetch = rt.count_fetches(m_last)
+    with roofline_range():
+        pass_ms = rt.time_pass(m_last, 5)
+    rt.close()
+    cm.close()
+
+    # end to end (e2e): the same frames from a fresh cache through the public
+    # API, every frame's RGBA8 image delivered to pinned host memory inside
+    # RenderFrame (rayt_renderer_set_host_image), wall clock per frame
+    pinned = torch.empty((h, w, 4), dtype=torch.uint8).pin_memory()
+    cm, rt, _ = renderer(host_image=pinned)
+    stream = torch.cuda.ExternalStream(rt.stream_handle())
+    torch.cuda.synchronize()
+    barrier(world)
+    wall, d2h = 0.0, 0
+    for i in range(args.warmup, args.warmup + steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(i & 255)
+        stream.synchronize()
+        t = time.perf_counter()
+        rt.RenderFrame(mats[i])
+        wall += time.perf_counter() - t
+        if len(timed_imgs) < args.parity_frames:
+            timed_imgs.append(pinned.numpy().copy())
+        d2h += rt.stats()["bytes_d2h"]  # the image and the feedback read-backs
+    torch.cuda.synchronize()
     barrier(world)
     clk = clocks.stop()
-    cs1 = cm.stats()
+    rt.close()
+    cm.close()
     t_dev = max_over_ranks(ms_dev / 1e3, world)
     t_wall = max_over_ranks(wall, world)
+    t_wall_after = max_over_ranks(wall_after, world)
     rays = float(w * h * steps)
     total_rays = sum_over_ranks(rays, world)
     # block streaming over the timed frames: block content and patches moved
@@ -518,11 +559,6 @@ def bench_frames(args, rank, world, local):
                  "block_source": "block file mapped into host memory, read by the upload kernel"
                                  if cs1["mapped"] else "pread into pinned staging, one copy per batch"}
 
-    # roofline of the dominant kernel (first-pass traversal) on the last camera
-    m_last = mats[args.warmup + steps - 1]
-    fetch = rt.count_fetches(m_last)
-    with roofline_range():
-        pass_ms = rt.time_pass(m_last, 5)
     alg_bytes = 4 * fetch["link_fetches"] + 4 * fetch["far_fetches"] + 16 * fetch["rays"]
     achieved = alg_bytes / (pass_ms / 1e3) / 1e9
     peak, peak_kind = hbm_peak()
@@ -547,11 +583,14 @@ def bench_frames(args, rank, world, local):
         "warmup": args.warmup, "ms_per_step": round(t_dev / steps * 1e3, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": wl, "width": w, "height": h, "depth": cfg["depth"], "spheres": cfg["spheres"],
-                   "nodes_in_block": 4096, "cache_blocks": cm.blocks()[1], "tree_blocks": ld.info.blocks_count,
+                   "nodes_in_block": 4096, "cache_blocks": n_cache_blocks, "tree_blocks": ld.info.blocks_count,
                    "lod_voxel_size": cfg["lod"], "l2": "flushed between frames (256 MiB write)",
                    "parallelism": "replicas" if world > 1 else "single GPU", "initial_fill_s": round(fill_s, 2)},
         "e2e": {"value": round(total_rays / t_wall / 1e6, 3), "unit": "Mrays/s",
-                "h2d_bytes_per_step": int(h2d / steps) + 64, "d2h_bytes_per_step": int(d2h / steps)},
+                "h2d_bytes_per_step": int(h2d / steps) + 64, "d2h_bytes_per_step": int(d2h / steps),
+                "how": "wall clock around RenderFrame with the image delivered to pinned host memory inside the call"},
+        "e2e_read_after": {"value": round(total_rays / t_wall_after / 1e6, 3), "unit": "Mrays/s",
+                           "how": "wall clock around RenderFrame and a read-back of the image after it returns"},
         "frame_latency_ms": {"p50": round(float(np.percentile(lat_sorted, 50)), 4),
                              "p99": round(float(np.percentile(lat_sorted, 99)), 4)},
         "frames": {"passes_per_frame": round(passes / steps, 3), "uploaded_blocks_per_frame": round(uploaded / steps, 2),

@@ -239,6 +239,18 @@ int rayt_renderer_pass_words(rayt_renderer* r, int pass, int32_t* host_words, si
  *             ray still faulted at the end - -1 for a miss, -2 for an error.
  * Turning it on allocates both buffers (and 4 bytes per ray record). */
 int rayt_renderer_set_depth_output(rayt_renderer* r, int on);
+/* No counterpart in the reference (its out_image() is a device buffer that
+ * GPURayTracer's caller draws with OpenGL, gpu-ray-tracer.h:20).  Host
+ * delivery for a headless caller: from the next frame on, RenderFrame also
+ * leaves the frame's RGBA8 image (width * height * 4 bytes, row 0 at the
+ * bottom) in host_rgba by the time it returns, as rayt_renderer_read_image
+ * would copy it.  The first pass's pixels are copied on a separate stream
+ * while the host decodes feedback and streams blocks; the pixels that later
+ * passes and the finish write go to host_rgba as well.  host_rgba must be
+ * page-locked (cudaHostAlloc, or host memory registered with cudaHostRegister)
+ * and stay valid until delivery is switched off (NULL) or the renderer is
+ * destroyed; one-view renderers only.  The device image stays valid too. */
+int rayt_renderer_set_host_image(rayt_renderer* r, void* host_rgba, size_t bytes);
 /* Device pointers of view `view`'s depth (float) and hit-node (int32) buffers;
  * either out pointer may be NULL.  RAYT_E_STATE if depth output was never on. */
 int rayt_renderer_depth(rayt_renderer* r, int view, void** device_depth, void** device_hit_nodes);

@@ -146,6 +146,7 @@ def lib():
         "rayt_renderer_read_image": (i32, [vp, vp, C.c_size_t]),
         "rayt_renderer_pass_words": (i32, [vp, i32, vp, C.c_size_t]),
         "rayt_renderer_set_depth_output": (i32, [vp, i32]),
+        "rayt_renderer_set_host_image": (i32, [vp, vp, C.c_size_t]),
         "rayt_renderer_depth": (i32, [vp, i32, C.POINTER(vp), C.POINTER(vp)]),
         "rayt_renderer_read_depth": (i32, [vp, i32, C.POINTER(f32), C.POINTER(i32), C.c_size_t]),
         "rayt_renderer_stats": (i32, [vp, C.POINTER(FrameStats)]),
@@ -479,6 +480,13 @@ class GPURayTracer:
         out = np.zeros(sum(w * h for w, h in self.sizes), np.int32)
         _check(lib().rayt_renderer_pass_words(self._h, p, out.ctypes.data, out.size))
         return out
+
+    def set_host_image(self, address, nbytes=0):
+        """Host delivery (rayt_renderer_set_host_image): every frame from the
+        next one on also leaves its RGBA8 image at `address` (page-locked
+        host memory of at least width * height * 4 bytes, e.g. a pinned torch
+        tensor's data_ptr()) when RenderFrame returns; None switches it off."""
+        _check(lib().rayt_renderer_set_host_image(self._h, address or None, nbytes if address else 0))
 
     def set_depth_output(self, on=True):
         """Per-pixel depth and hit-node buffers from the next frame on (see

@@ -65,6 +65,7 @@ struct TraceParams {
   float bg[4];             // background colour (0, 216/255, 1, 1)
   // outputs of every view
   uchar4* image;           // RGBA8, row 0 of each view at the bottom
+  uchar4* host_image;      // optional: the same pixels also written here (page-locked host memory)
   int32_t* words_dense;    // optional per-pixel feedback words (recording)
   // first pass: the views of this launch and their tiles (32 rays each)
   int n_views;

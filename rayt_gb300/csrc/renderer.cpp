@@ -37,6 +37,7 @@ class Renderer {
   int ReadImage(int view, void* host, size_t bytes);
   int PassWords(int pass, int32_t* host, size_t count) const;
   int SetDepthOutput(bool on);
+  int SetHostImage(void* host, size_t bytes);
   int DepthBuffers(int view, float** depth, int32_t** nodes) const;
   int ReadDepth(int view, float* depth, int32_t* nodes, size_t count);
 
@@ -90,6 +91,13 @@ class Renderer {
   int* d_counts_ = nullptr;
   int32_t* h_dense_ = nullptr;       // pinned, for recording
   uint8_t* d_flush_ = nullptr;       // L2 flush buffer for TimePass
+  // Host delivery of the image (one view): the caller's page-locked buffer,
+  // its device address, a copy stream, and events "first pass done" (on the
+  // renderer's stream) and "its copy done" (on the copy stream).
+  uchar4* host_img_ = nullptr;
+  uchar4* host_img_dev_ = nullptr;
+  cudaStream_t copy_s_ = nullptr;
+  cudaEvent_t copy_ev_[2] = {};
   cudaEvent_t ev_[8] = {};
   std::vector<std::vector<int32_t>> pass_words_;
   FeedbackDecoder fb_;
@@ -133,6 +141,12 @@ void Renderer::DropGraphs() {
 
 Renderer::~Renderer() {
   if (s_) cudaStreamSynchronize(s_);
+  if (copy_s_) {
+    cudaStreamSynchronize(copy_s_);
+    cudaStreamDestroy(copy_s_);
+  }
+  for (auto& e : copy_ev_)
+    if (e) cudaEventDestroy(e);
   DropGraphs();
   cudaFree(d_images_);
   cudaFree(d_coords_);
@@ -256,6 +270,9 @@ TraceParams Renderer::Params(int it) const {
   p.bg[2] = 1.0f;
   p.bg[3] = 1.0f;
   p.image = d_images_;
+  // the first pass's pixels reach the host image by one copy; later passes
+  // write theirs there too
+  p.host_image = it > 0 ? host_img_dev_ : nullptr;
   p.words_dense = record ? d_dense_ : nullptr;
   p.tile_w_log2 = tile_w_log2;
   const RayList& in = lists_[1 - k];
@@ -467,8 +484,23 @@ int Renderer::Frame(const float* m) {
   using clock = std::chrono::steady_clock;
   auto ms_since = [](clock::time_point a) { return std::chrono::duration<double, std::milli>(clock::now() - a).count(); };
   int it;
+  bool copy_pending = false;  // the first pass's pixels on their way to the host image
   for (it = 0;; ++it) {
+    if (it > 0 && copy_pending) {  // later passes write host pixels only after the copy
+      RAYT_CUDA_TRY(cudaStreamWaitEvent(s_, copy_ev_[1], 0));
+      copy_pending = false;
+    }
     if ((rc = RunPass(it, active_prev, &launches)) != RAYT_OK) break;
+    if (it == 0 && host_img_) {
+      // the copy runs while the host decodes the feedback and streams blocks
+      const size_t bytes = (size_t)views_[0].width * views_[0].height * 4;
+      RAYT_CUDA_TRY(cudaEventRecord(copy_ev_[0], s_));
+      RAYT_CUDA_TRY(cudaStreamWaitEvent(copy_s_, copy_ev_[0], 0));
+      RAYT_CUDA_TRY(cudaMemcpyAsync(host_img_, d_images_, bytes, cudaMemcpyDeviceToHost, copy_s_));
+      RAYT_CUDA_TRY(cudaEventRecord(copy_ev_[1], copy_s_));
+      copy_pending = true;
+      d2h += (int64_t)bytes;
+    }
     if (record) {
       if (!h_dense_) RAYT_CUDA_TRY(cudaHostAlloc(&h_dense_, (size_t)padded_pixels_ * 4, cudaHostAllocDefault));
       RAYT_CUDA_TRY(cudaMemcpyAsync(h_dense_, d_dense_, (size_t)padded_pixels_ * 4, cudaMemcpyDeviceToHost, s_));
@@ -524,6 +556,7 @@ int Renderer::Frame(const float* m) {
   }
   if (cache_->in_transaction()) cache_->EndTransaction();
   const int src = cache_->EndSession();
+  if ((rc != RAYT_OK || src != RAYT_OK) && copy_pending) cudaStreamSynchronize(copy_s_);
   if (rc != RAYT_OK) return rc;
   if (src != RAYT_OK) return src;
   // FinishTracingFrame for the rays still faulted, against the cache as it is now
@@ -535,6 +568,8 @@ int Renderer::Frame(const float* m) {
   f.in_ray = p.out_ray;
   f.in_adv = p.out_adv;
   f.n_in = p.n_out;
+  f.host_image = host_img_dev_;
+  if (copy_pending) RAYT_CUDA_TRY(cudaStreamWaitEvent(s_, copy_ev_[1], 0));  // also ends with the copy
   RAYT_CUDA_TRY(launch_finish(f, active_prev, s_));
   if (active_prev > 0) ++launches;
   const auto tw = clock::now();
@@ -622,6 +657,40 @@ int Renderer::Autotune(const float* m, int reps, int* best) {
   step_budget = b[3];
   if (best)
     for (int k = 0; k < 4; ++k) best[k] = b[k];
+  return RAYT_OK;
+}
+
+// Host delivery: every frame's image also lands in `host` by the time the
+// frame returns.  The buffer must be page-locked (cudaHostAlloc or
+// cudaHostRegister): the copy engine and the traversal kernels write it
+// directly.
+int Renderer::SetHostImage(void* host, size_t bytes) {
+  if (!host) {
+    if (copy_s_) RAYT_CUDA_TRY(cudaStreamSynchronize(copy_s_));
+    host_img_ = host_img_dev_ = nullptr;
+    return RAYT_OK;
+  }
+  if (n_views() != 1) return fail(RAYT_E_ARG, "host image delivery needs a one-view renderer");
+  if (bytes < (size_t)views_[0].width * views_[0].height * 4) return fail(RAYT_E_ARG, "host image buffer too small");
+  // page-locked memory only (the runtime reports it as host memory; on a
+  // system where the device also reaches pageable memory, a copy into that
+  // would hold the calling thread until the copy ends)
+  cudaPointerAttributes a{};
+  void* dev = nullptr;
+  if (cudaPointerGetAttributes(&a, host) == cudaSuccess && a.type == cudaMemoryTypeHost) {
+    dev = a.devicePointer;
+    if (!dev && cudaHostGetDevicePointer(&dev, host, 0) != cudaSuccess) dev = nullptr;
+  }
+  cudaGetLastError();
+  if (!dev) return fail(RAYT_E_ARG, "host image must be page-locked memory (cudaHostAlloc or cudaHostRegister)");
+  if (!copy_s_) {
+    RAYT_CUDA_TRY(cudaStreamCreateWithFlags(&copy_s_, cudaStreamNonBlocking));
+    for (auto& e : copy_ev_) RAYT_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  RAYT_CUDA_TRY(cudaStreamSynchronize(s_));  // no frame writes the old buffer any more
+  RAYT_CUDA_TRY(cudaStreamSynchronize(copy_s_));
+  host_img_ = static_cast<uchar4*>(host);
+  host_img_dev_ = static_cast<uchar4*>(dev);
   return RAYT_OK;
 }
 
@@ -817,6 +886,9 @@ int rayt_renderer_read_image(rayt_renderer* r, void* host, size_t bytes) {
 int rayt_renderer_pass_words(rayt_renderer* r, int pass, int32_t* host, size_t count) {
   if (!r || !host) return fail(RAYT_E_ARG, "null argument");
   return R(r)->PassWords(pass, host, count);
+}
+int rayt_renderer_set_host_image(rayt_renderer* r, void* host_rgba, size_t bytes) {
+  return r ? R(r)->SetHostImage(host_rgba, bytes) : fail(RAYT_E_ARG, "null renderer");
 }
 int rayt_renderer_set_depth_output(rayt_renderer* r, int on) {
   if (!r) return fail(RAYT_E_ARG, "null renderer");

@@ -593,6 +593,14 @@ __device__ __forceinline__ void write_depth(const TraceParams& p, uint32_t ray, 
 constexpr uint32_t kDepthNaN = 0x7fffffffu;
 constexpr uint32_t kDepthInf = 0x7f800000u;
 
+// A final pixel: into the image, and into the caller's host image when the
+// renderer delivers one (later passes and the finish; the first pass's pixels
+// reach it by one copy).
+__device__ __forceinline__ void put_pixel(const TraceParams& p, uint32_t ray, uchar4 px) {
+  p.image[ray] = px;
+  if (p.host_image) p.host_image[ray] = px;
+}
+
 // RaytracingPass's handling of an ended ray (raytracing_pass.cl:20-58) plus
 // FinishTracingFrame for rays that end here: the final pixel, the next pass's
 // record of a faulted ray, the feedback bitmaps and counters.  Called by the
@@ -606,16 +614,16 @@ __device__ __forceinline__ void end_ray(const TraceParams& p, const RayEnd& e, u
   const int node = e.node, dup = e.dup, fault_block = e.fault_block;
   int32_t word = kNoHit;
   if (e.error) {
-    p.image[ray] = finish(p, make_uchar4(255, 0, 0, 255));
+    put_pixel(p, ray, finish(p, make_uchar4(255, 0, 0, 255)));
     if (p.depth) write_depth(p, ray, __uint_as_float(kDepthNaN), -2);
   } else if (faulted) {
     word = -fault_block - 1;
   } else if (!hit) {
-    p.image[ray] = finish(p, make_uchar4(0, 0, 0, 0));
+    put_pixel(p, ray, finish(p, make_uchar4(0, 0, 0, 0)));
     if (p.depth) write_depth(p, ray, __uint_as_float(kDepthInf), -1);
   } else {
     const uchar4 col = (p.normals && p.colors) ? shade(p, (uint32_t)node) : make_uchar4(0, 0, 0, 0);
-    p.image[ray] = finish(p, col);
+    put_pixel(p, ray, finish(p, col));
     word = (int32_t)(((uint32_t)(node + 1) << 1) | (uint32_t)dup);
     if (p.depth) write_depth(p, ray, adv + e.t, node);
   }
@@ -753,7 +761,7 @@ __global__ void __launch_bounds__(kBlockThreads) trace_queue_kernel(const __grid
         // served mode: the request stops here; FinishTracingFrame's shading
         // with the fault's parent node
         const uchar4 col = (p.normals && p.colors) ? shade(p, (uint32_t)p.in_parent[r]) : make_uchar4(0, 0, 0, 0);
-        p.image[ray] = finish(p, col);
+        put_pixel(p, ray, finish(p, col));
         if (p.depth) write_depth(p, ray, adv, p.in_parent[r]);
       } else {
         uint32_t fetches = 0, far_fetches = 0;
@@ -771,7 +779,7 @@ __global__ void __launch_bounds__(kBlockThreads) finish_kernel(const __grid_cons
   const int i = blockIdx.x * kBlockThreads + threadIdx.x;
   if (i >= *p.n_in) return;
   const uchar4 col = (p.normals && p.colors) ? shade(p, (uint32_t)p.in_parent[i]) : make_uchar4(0, 0, 0, 0);
-  p.image[p.in_ray[i]] = finish(p, col);
+  put_pixel(p, p.in_ray[i], finish(p, col));
   if (p.depth) write_depth(p, p.in_ray[i], p.in_adv[i], p.in_parent[i]);
 }
 
