@@ -945,32 +945,35 @@ def bench_served(args, rank, world, local):
     pinned = [torch.empty((h, w, 4), dtype=torch.uint8).pin_memory() for w, h in sizes]
     rts = []
 
-    def plain_renderers():
+    def plain_renderers(deliver):
+        """One renderer per client on a fresh cache; with deliver, each frame's
+        image lands in the client's pinned buffer inside RenderFrame, as the
+        server delivers (rayt_renderer_set_host_image)."""
         for rt in rts:
             rt.close()
         rts.clear()
         c = fresh_cache()
-        for (w, h) in sizes:
+        for k, (w, h) in enumerate(sizes):
             rt = R.GPURayTracer(c, w, h)
             rt.set_lod_voxel_size(cfg["lod"])
             rt.set_frame_time_limit(1e30)
             rt.set_max_passes(cfg["max_passes"])
+            if deliver:
+                rt.set_host_image(pinned[k].data_ptr(), pinned[k].numel())
             rts.append(rt)
         return c
 
-    def plain_frame(c, f, deliver=True):
+    def plain_frame(c, f):
         rts[c].RenderFrame(cams[c][f])
-        if deliver:
-            R._check(R.lib().rayt_renderer_read_image(rts[c]._h, pinned[c].data_ptr(), pinned[c].numel()))
 
     def closed_plain(deliver, cap_s):
         """The same frames in the same order, one RenderFrame each, from the
         same cache state (fresh cache, the same warm-up frames)."""
-        pc = plain_renderers()
+        pc = plain_renderers(deliver)
         up0 = pc.stats()["uploaded_blocks"]
         for f in range(args.warmup):
             for c in range(nclients):
-                plain_frame(c, f, deliver)
+                plain_frame(c, f)
         torch.cuda.synchronize()
         n, t_end = 0, time.perf_counter() + cap_s
         up1 = pc.stats()["uploaded_blocks"]
@@ -979,7 +982,7 @@ def bench_served(args, rank, world, local):
             if time.perf_counter() > t_end:
                 break
             for c in range(nclients):
-                plain_frame(c, f, deliver)
+                plain_frame(c, f)
                 n += 1
         torch.cuda.synchronize()
         return n, time.perf_counter() - t, pc.stats()["uploaded_blocks"] - up1
@@ -988,7 +991,7 @@ def bench_served(args, rank, world, local):
     n_plain_e2e, el_plain_e2e, _ = closed_plain(True, 60)
     log("plain closed loop: %d frames in %.3fs, %d blocks uploaded (%d in %.3fs delivered)"
         % (n_plain, el_plain, up_plain, n_plain_e2e, el_plain_e2e))
-    plain_renderers()
+    plain_renderers(True)
     lat_plain = []
     t_start = time.perf_counter()
     for (t, c, f) in sched:

@@ -340,7 +340,9 @@ typedef struct {
   int64_t max_rays_in_flight;  /* ray records held between passes (request admission) */
   int max_passes;              /* tracing passes per request before its faulted rays are shaded */
   float lod_voxel_size;
-  int deliver_to_host;         /* copy every finished frame to the client's pinned host image */
+  int deliver_to_host;         /* copy every finished frame to the client's pinned host image
+                                  (a request is done once its image is there; the copies
+                                  overlap the following ticks) */
 } rayt_server_config;
 typedef struct {
   uint64_t request;

@@ -25,6 +25,7 @@
 #include <cstring>
 #include <deque>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <unordered_map>
@@ -68,6 +69,7 @@ class Server {
     int64_t pixels = 0;      // w * h rounded up to 64
     uint64_t in_flight = 0;  // request being rendered (0: none)
     uchar4* host = nullptr;  // pinned copy of the last finished frame (deliver_to_host)
+    uchar4* stage = nullptr; // device copy of a finished frame on its way to `host`
     float* coords = nullptr; // pixel_coords(w, h) in device memory
   };
   struct Request {
@@ -103,6 +105,19 @@ class Server {
   int* d_client_faults_ = nullptr;
   int tick_ = 0;
   int carried_ = 0;          // faulted rays carried into the next tick
+  // deliver_to_host: finished frames are copied to their client's stage on
+  // the GPU stream (the framebuffer is free for the client's next request
+  // right after), and from there to the pinned host image on a copy stream
+  // while the next ticks run; a host function on the copy stream records the
+  // requests as done once their images are on the host.
+  cudaStream_t copy_s_ = nullptr;
+  cudaEvent_t staged_ev_ = nullptr, copied_ev_ = nullptr;
+  bool copy_pending_ = false;  // copied_ev_ marks the last delivery
+  struct Delivery {
+    Server* server;
+    std::vector<rayt_request_info> done;
+  };
+  static void CUDART_CB Delivered(void* delivery);
   FeedbackDecoder fb_;
   std::vector<Client> clients_;
   std::vector<Flight> flights_;
@@ -151,6 +166,11 @@ int Server::Init(Cache* cache, const rayt_server_config& cfg) {
   RAYT_CUDA_TRY(cudaHostGetDevicePointer((void**)&d_counts_, h_counts_, 0));
   RAYT_CUDA_TRY(cudaMemsetAsync(d_state_, 0, words * 4, s_));
   RAYT_CUDA_TRY(cudaMemsetAsync(d_images_, 0, image_pixels_ * 4, s_));
+  if (cfg.deliver_to_host) {
+    RAYT_CUDA_TRY(cudaStreamCreateWithFlags(&copy_s_, cudaStreamNonBlocking));
+    RAYT_CUDA_TRY(cudaEventCreateWithFlags(&staged_ev_, cudaEventDisableTiming));
+    RAYT_CUDA_TRY(cudaEventCreateWithFlags(&copied_ev_, cudaEventDisableTiming));
+  }
   RAYT_CUDA_TRY(cudaStreamSynchronize(s_));
   return RAYT_OK;
 }
@@ -158,6 +178,12 @@ int Server::Init(Cache* cache, const rayt_server_config& cfg) {
 Server::~Server() {
   Stop();
   if (s_) cudaStreamSynchronize(s_);
+  if (copy_s_) {
+    cudaStreamSynchronize(copy_s_);  // deliveries and their host functions end
+    cudaStreamDestroy(copy_s_);
+  }
+  if (staged_ev_) cudaEventDestroy(staged_ev_);
+  if (copied_ev_) cudaEventDestroy(copied_ev_);
   cudaFree(d_images_);
   for (auto& l : lists_) {
     cudaFree(l.origin);
@@ -170,8 +196,22 @@ Server::~Server() {
   cudaFreeHost(h_counts_);
   for (auto& c : clients_) {
     if (c.host) cudaFreeHost(c.host);
+    cudaFree(c.stage);
     cudaFree(c.coords);
   }
+}
+
+void CUDART_CB Server::Delivered(void* delivery) {
+  std::unique_ptr<Delivery> d(static_cast<Delivery*>(delivery));
+  Server* s = d->server;
+  const double t = now_s();
+  std::lock_guard<std::mutex> lock(s->mu_);
+  for (rayt_request_info& info : d->done) {
+    info.done_s = std::max(info.done_s, t);
+    s->done_[info.request] = info;
+    ++s->stats.completed;
+  }
+  s->cv_.notify_all();
 }
 
 // First fit in the framebuffer pool (ranges ordered by base).
@@ -207,6 +247,12 @@ int Server::AddClient(int w, int h, int* id) {
   if (cfg_.deliver_to_host && !c.host &&
       cudaHostAlloc(&c.host, (size_t)w * h * 4, cudaHostAllocDefault) != cudaSuccess)
     return fail(RAYT_E_OOM, "pinned host image allocation failed");
+  if (cfg_.deliver_to_host) {
+    if (copy_s_) RAYT_CUDA_TRY(cudaStreamSynchronize(copy_s_));  // an earlier client's stage may still be read
+    cudaFree(c.stage);
+    c.stage = nullptr;
+    if (cudaMalloc(&c.stage, (size_t)w * h * 4) != cudaSuccess) return fail(RAYT_E_OOM, "delivery stage allocation failed");
+  }
   std::vector<float> coords(pixel_coords_count(w, h));
   pixel_coords(w, h, coords.data());
   cudaFree(c.coords);
@@ -228,12 +274,16 @@ int Server::RemoveClient(int id) {
   if (id < 0 || id >= (int)clients_.size() || !clients_[id].live) return fail(RAYT_E_ARG, "no such client");
   if (running_) return fail(RAYT_E_ARG, "remove clients while the scheduler thread is stopped");
   if (clients_[id].in_flight) return fail(RAYT_E_ARG, "client has a frame in flight");
+  // its last delivery ends first (not under mu_: the delivery's host function takes it)
+  if (copy_s_) RAYT_CUDA_TRY(cudaStreamSynchronize(copy_s_));
   std::lock_guard<std::mutex> lock(mu_);
   for (const Request& r : queue_)
     if (r.client == id) return fail(RAYT_E_ARG, "client has queued frames");
   clients_[id].live = false;
   if (clients_[id].host) cudaFreeHost(clients_[id].host);
   clients_[id].host = nullptr;
+  cudaFree(clients_[id].stage);
+  clients_[id].stage = nullptr;
   cudaFree(clients_[id].coords);
   clients_[id].coords = nullptr;
   return RAYT_OK;
@@ -455,13 +505,26 @@ int Server::Step(int* finished) {
 
   // deliver and record the requests that ended
   if (!ended.empty()) {
+    std::unique_ptr<Delivery> delivery;
     if (cfg_.deliver_to_host) {
+      // frames to their stages (after the previous delivery has read them),
+      // then to the host on the copy stream; the framebuffers are free for the
+      // clients' next requests in stream order
+      delivery.reset(new Delivery{this, {}});
+      if (copy_pending_) RAYT_CUDA_TRY(cudaStreamWaitEvent(s_, copied_ev_, 0));
       for (const Flight& f : ended) {
         const Client& c = clients_[f.client];
-        RAYT_CUDA_TRY(cudaMemcpyAsync(c.host, d_images_ + c.base, (size_t)c.w * c.h * 4, cudaMemcpyDeviceToHost, s_));
+        RAYT_CUDA_TRY(cudaMemcpyAsync(c.stage, d_images_ + c.base, (size_t)c.w * c.h * 4, cudaMemcpyDeviceToDevice, s_));
+      }
+      RAYT_CUDA_TRY(cudaEventRecord(staged_ev_, s_));
+      RAYT_CUDA_TRY(cudaStreamWaitEvent(copy_s_, staged_ev_, 0));
+      for (const Flight& f : ended) {
+        const Client& c = clients_[f.client];
+        RAYT_CUDA_TRY(cudaMemcpyAsync(c.host, c.stage, (size_t)c.w * c.h * 4, cudaMemcpyDeviceToHost, copy_s_));
         stats.bytes_d2h += (int64_t)c.w * c.h * 4;
       }
-      RAYT_CUDA_TRY(cudaStreamSynchronize(s_));
+      RAYT_CUDA_TRY(cudaEventRecord(copied_ev_, copy_s_));
+      copy_pending_ = true;
     }
     const double t_done = now_s();
     std::lock_guard<std::mutex> lock(mu_);
@@ -474,12 +537,21 @@ int Server::Step(int* finished) {
       info.submit_s = f.submit_s;
       info.admit_s = f.admit_s;
       info.done_s = std::max(t_pass, t_done);
-      done_[f.id] = info;
+      if (delivery) {
+        delivery->done.push_back(info);  // done once the image is on the host
+      } else {
+        done_[f.id] = info;
+        ++stats.completed;
+      }
       clients_[f.client].in_flight = 0;
       reserved_ -= f.rays;
-      ++stats.completed;
     }
-    cv_.notify_all();
+    if (delivery) {
+      RAYT_CUDA_TRY(cudaLaunchHostFunc(copy_s_, &Server::Delivered, delivery.get()));
+      delivery.release();  // the host function owns it now
+    } else {
+      cv_.notify_all();
+    }
   }
   if (finished) *finished = (int)ended.size();
   return RAYT_OK;
@@ -551,8 +623,10 @@ int Server::Wait(uint64_t request, double timeout_s, rayt_request_info* out) {
       }
     }
     if (now_s() > deadline) return fail(RAYT_E_TIMEOUT, "request not finished before the timeout");
+    const bool idle = flights_.empty();
     const int rc = Step(nullptr);  // no scheduler thread: run ticks here
     if (rc != RAYT_OK) return rc;
+    if (idle && copy_s_) RAYT_CUDA_TRY(cudaStreamSynchronize(copy_s_));  // a delivery still on its way
   }
 }
 
