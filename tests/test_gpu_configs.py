@@ -23,7 +23,7 @@ from tests.conftest import libc_srand
 
 pytestmark = pytest.mark.gpu
 
-DRIVER_FRAMES = 25  # frames of a short run: 5 warm-up + 20 timed
+SHORT_RUN_FRAMES = 25  # frames of a short run: 5 warm-up + 20 timed
 
 
 @pytest.fixture(scope="module")
@@ -53,7 +53,7 @@ def test_c3_streamed_frames_vs_oracle(c3_scene):
     cfg = bench.WORKLOADS["c3"]
     # the whole spline in 25 frames: each frame moves 12x as far as in the
     # 300-frame flythrough, so every frame streams hundreds of blocks
-    mats = bench.camera_path("c3", DRIVER_FRAMES, cfg["width"], cfg["height"], period=DRIVER_FRAMES)[:4]
+    mats = bench.camera_path("c3", SHORT_RUN_FRAMES, cfg["width"], cfg["height"], period=SHORT_RUN_FRAMES)[:4]
     out = bench.frames_parity(c3_scene, cfg, mats, seed=1)
     assert out["frames"] == 4 and out["uploaded_blocks"] > 0
     assert out["passes"] > out["frames"]  # frames streamed blocks and traced again
@@ -64,7 +64,7 @@ def test_c4_batched_frame_vs_oracle(c3_scene, resident_oracle):
     cfg = bench.WORKLOADS["c4"]
     sizes, seeds = bench.batched_views(cfg)
     f = 5  # the first timed frame of the benchmark's default run
-    mats = [bench.camera_path("c4", DRIVER_FRAMES, w, h, seed=sd)[f] for (w, h), sd in zip(sizes, seeds)]
+    mats = [bench.camera_path("c4", SHORT_RUN_FRAMES, w, h, seed=sd)[f] for (w, h), sd in zip(sizes, seeds)]
     ld = R.StoredOctreeLoader(c3_scene)
     cm = R.GPUOctreeCacheManager(0, ld)
     cm.InitialFillCache()
@@ -90,7 +90,7 @@ def test_c5_client_size_mix_vs_oracle(c3_scene, resident_oracle):
     the depth-12 tree (so their frames fault and share ticks): each request's
     image equals the oracle's resident one-view frame of its camera."""
     sizes = [(1280, 720), (1920, 1080), (2560, 1440)]
-    cams = [bench.camera_path("c3", DRIVER_FRAMES, w, h, seed=100 + c) for c, (w, h) in enumerate(sizes)]
+    cams = [bench.camera_path("c3", SHORT_RUN_FRAMES, w, h, seed=100 + c) for c, (w, h) in enumerate(sizes)]
     ld = R.StoredOctreeLoader(c3_scene)
     cm = R.GPUOctreeCacheManager(bench.cache_blocks(bench.WORKLOADS["c3"]), ld)
     cm.InitialFillCache()
