@@ -54,3 +54,22 @@ def test_two_gloo_ranks(tmp_path, built):
     assert [r[1] for r in res] == [2.0, 2.0]      # max over ranks
     assert [r[2] for r in res] == [30.0, 30.0]    # sum over ranks
     assert all(r[3] for r in res) and res[0][4] == res[1][4] > 0  # one scene, seen by both
+
+
+def test_flythrough_frames_sit_at_the_configured_spacing(built):
+    """c3 is 300 frames along one loop of its spline: a run of any length
+    renders the first frames of that flythrough at the same spacing (the
+    cameras of a 25-frame run are the first 25 of a 303-frame run), frame i
+    wraps around the closed loop after 300, and a period equal to the run
+    spreads the run over the whole loop."""
+    sys.path.insert(0, ROOT)
+    import numpy as np
+    import bench as B
+    w, h = 1920, 1080
+    short = B.camera_path("c3", 25, w, h, period=B.C3_PATH_FRAMES)
+    long_ = B.camera_path("c3", 303, w, h, period=B.C3_PATH_FRAMES)
+    assert np.array_equal(np.array(short), np.array(long_[:25]))
+    assert np.array_equal(np.array(long_[300:303]), np.array(long_[0:3]))
+    loop = B.camera_path("c3", 25, w, h)
+    assert np.array_equal(np.array(loop[0]), np.array(short[0]))
+    assert not np.array_equal(np.array(loop[1]), np.array(short[1]))  # 12x the camera motion per frame
