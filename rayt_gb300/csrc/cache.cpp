@@ -972,7 +972,7 @@ int rayt_cache_create(rayt_tree* tree, int max_blocks, rayt_cache** out) {
   *out = reinterpret_cast<rayt_cache*>(c);
   return RAYT_OK;
 }
-void rayt_cache_destroy(rayt_cache* c) { delete C(c); }
+void rayt_cache_destroy(rayt_cache* c) { rayt::Cache::Release(C(c)); }
 int rayt_cache_initial_fill(rayt_cache* c) { return c ? C(c)->InitialFill() : fail(RAYT_E_ARG, "null cache"); }
 int rayt_cache_root_node_index(const rayt_cache* c, int* out) {
   if (!c || !out) return fail(RAYT_E_ARG, "null argument");

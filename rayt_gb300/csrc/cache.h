@@ -74,6 +74,12 @@ class Cache {
  public:
   ~Cache();
   int Init(Tree* tree, int max_blocks);
+  // Reference count: the creator holds one; every renderer and server on the
+  // cache holds one, so whichever is released last frees it.
+  void Retain() { refs_.fetch_add(1); }
+  static void Release(Cache* c) {
+    if (c && c->refs_.fetch_sub(1) == 1) delete c;
+  }
 
   // GPUOctreeCacheManager protocol
   int InitialFill();
@@ -125,6 +131,7 @@ class Cache {
     bool live = false;
   };
 
+  std::atomic<int> refs_{1};
   Tree* tree_ = nullptr;
   int nib_ = 0, max_blocks_ = 0, first_free_ = 0;
   uint32_t root_node_ = 0;   // node index: below 2^32 (caches hold fewer than 2^32 nodes)

@@ -168,10 +168,12 @@ Renderer::~Renderer() {
   cudaFreeHost(h_dense_);
   for (auto& e : ev_)
     if (e) cudaEventDestroy(e);
+  Cache::Release(cache_);
 }
 
 int Renderer::Init(Cache* cache, int n_views, const int* widths, const int* heights) {
   if (n_views < 1 || n_views > kMaxViews) return fail(RAYT_E_ARG, "view count out of range (1..512)");
+  cache->Retain();  // the cache (its stream and buffers) outlives this renderer
   cache_ = cache;
   s_ = cache->stream();
   views_.assign(n_views, ViewDesc{});

@@ -143,6 +143,7 @@ int Server::Init(Cache* cache, const rayt_server_config& cfg) {
       cfg.max_passes < 1 || !(cfg.lod_voxel_size >= 0))
     return fail(RAYT_E_ARG, "bad server configuration");
   cfg_ = cfg;
+  cache->Retain();  // the cache (its stream and buffers) outlives this server
   cache_ = cache;
   s_ = cache->stream();
   image_pixels_ = std::min<int64_t>(cfg.framebuffer_bytes / 4, 1ll << 30) & ~(int64_t)63;
@@ -199,6 +200,7 @@ Server::~Server() {
     cudaFree(c.stage);
     cudaFree(c.coords);
   }
+  Cache::Release(cache_);
 }
 
 void CUDART_CB Server::Delivered(void* delivery) {
@@ -354,9 +356,10 @@ TraceParams Server::Params(int k) const {
 // One tick: admit, one pass over everything in flight, feedback, transaction.
 int Server::Step(int* finished) {
   if (finished) *finished = 0;
-  const double t_admit = now_s();
   {
     std::lock_guard<std::mutex> lock(mu_);
+    // under the lock: every request admitted here was submitted before
+    const double t_admit = now_s();
     for (auto it = queue_.begin(); it != queue_.end();) {
       Client& c = clients_[it->client];
       const int64_t rays = (int64_t)c.w * c.h;

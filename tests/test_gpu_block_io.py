@@ -103,6 +103,40 @@ def test_tree_closed_before_its_cache(trees):
         np.testing.assert_array_equal(a, b, err_msg="frame %d" % i)
 
 
+def test_cache_released_before_its_renderer_and_server(trees):
+    """Releasing the cache handle while a renderer or a server still uses it
+    is allowed: each keeps the cache (its stream and buffers) until it is
+    destroyed.  Frames after the release equal frames with it kept."""
+    w, h = 160, 90
+    mats = [R.Camera(a, -30.0, 0.0, (0.5 - 0.6 * np.sin(np.radians(a)), 0.7, 0.5 + 0.6 * np.cos(np.radians(a))),
+                     60.0, w / h).view_proj_inv() for a in range(0, 360, 90)]
+    images = []
+    for release_early in (False, True):
+        ld, cm = _cache(trees["terrain8s"], 250, "mapped")
+        cm.InitialFillCache()
+        rt = R.GPURayTracer(cm, w, h)
+        rt.set_frame_time_limit(1e30)
+        rt.seed(3)
+        srv = R.RenderServer(cm, max_clients=2, framebuffer_bytes=w * h * 8, max_rays_in_flight=w * h * 2,
+                             deliver_to_host=True)
+        client = srv.add_client(w, h)
+        if release_early:
+            cm.close()
+            ld.close()
+        run = []
+        for m in mats:
+            rt.RenderFrame(m)
+            run.append(rt.read_image().copy())
+            srv.wait(srv.submit(client, m), timeout=60)
+            run.append(srv.host_image(client).copy())
+        images.append(run)
+        srv.close()
+        rt.close()
+        cm.close()
+    for i, (a, b) in enumerate(zip(*images)):
+        np.testing.assert_array_equal(a, b, err_msg="image %d" % i)
+
+
 def _write_tree(path, nib, extra_name, extra_bytes, rng):
     """A one-block tree: 'node links' (in-block child links and empty nodes)
     and one more channel; the channel name's length moves the block record's
