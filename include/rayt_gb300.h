@@ -247,9 +247,10 @@ int rayt_renderer_set_depth_output(rayt_renderer* r, int on);
  * would copy it.  The first pass's pixels are copied on a separate stream
  * while the host decodes feedback and streams blocks; the pixels that later
  * passes and the finish write go to host_rgba as well.  host_rgba must be
- * page-locked (cudaHostAlloc, or host memory registered with cudaHostRegister)
- * and stay valid until delivery is switched off (NULL) or the renderer is
- * destroyed; one-view renderers only.  The device image stays valid too. */
+ * page-locked (cudaHostAlloc, or host memory registered with cudaHostRegister),
+ * 4-byte aligned, and stay valid until delivery is switched off (NULL) or the
+ * renderer is destroyed; one-view renderers only.  The device image stays
+ * valid too. */
 int rayt_renderer_set_host_image(rayt_renderer* r, void* host_rgba, size_t bytes);
 /* Device pointers of view `view`'s depth (float) and hit-node (int32) buffers;
  * either out pointer may be NULL.  RAYT_E_STATE if depth output was never on. */

@@ -674,6 +674,7 @@ int Renderer::SetHostImage(void* host, size_t bytes) {
   }
   if (n_views() != 1) return fail(RAYT_E_ARG, "host image delivery needs a one-view renderer");
   if (bytes < (size_t)views_[0].width * views_[0].height * 4) return fail(RAYT_E_ARG, "host image buffer too small");
+  if (reinterpret_cast<uintptr_t>(host) & 3u) return fail(RAYT_E_ARG, "host image must be 4-byte aligned (RGBA8 pixels)");
   // page-locked memory only (the runtime reports it as host memory; on a
   // system where the device also reaches pageable memory, a copy into that
   // would hold the calling thread until the copy ends)

@@ -80,9 +80,11 @@ def test_host_image_refuses_pageable_memory_and_views(trees):
     pageable = np.zeros(w * h * 4, np.uint8)
     with pytest.raises(R.RaytError):
         rt.set_host_image(pageable.ctypes.data, pageable.nbytes)
-    buf = _pinned(w * h * 4)
+    buf = _pinned(w * h * 4 + 4)
     with pytest.raises(R.RaytError):
         rt.set_host_image(buf.data_ptr(), w * h * 4 - 1)
+    with pytest.raises(R.RaytError):  # pixels are written as 4-byte words
+        rt.set_host_image(buf.data_ptr() + 1, w * h * 4)
     views = R.GPURayTracer.views(cm, [(w, h), (32, 32)])
     with pytest.raises(R.RaytError):
         views.set_host_image(buf.data_ptr(), buf.numel())
