@@ -84,7 +84,10 @@ class Cache {
   // GPUOctreeCacheManager protocol
   int InitialFill();
   int StartSession();
-  int StartTransaction();
+  // expected_requests: the blocks the caller is about to request, when it
+  // knows (a transaction that small reads them on the calling thread, so the
+  // read pool is not woken for it); -1 when it does not.
+  int StartTransaction(int expected_requests = -1);
   int MarkBlockUsed(int slot);
   int MarkParentUsed(int slot);
   // MarkBlockUsed for every slot of hits, then MarkParentUsed for every slot

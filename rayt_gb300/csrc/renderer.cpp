@@ -533,7 +533,7 @@ int Renderer::Frame(const float* m) {
 
     const auto td = clock::now();
     fb_.Decode(h_unique_, h_counts_[0], rand);
-    if ((rc = cache_->StartTransaction()) != RAYT_OK) break;
+    if ((rc = cache_->StartTransaction((int)fb_.faults.size())) != RAYT_OK) break;
     cache_->MarkUsedBatch(fb_.hits, fb_.dup_hits);
     for (int f : fb_.faults) {
       if (cache_->TransactionFilled()) break;

@@ -479,7 +479,7 @@ int Server::Step(int* finished) {
   const int64_t uploaded0 = cache_->stats().uploaded_blocks;
   fb_.Decode(h_unique_, h_counts_[0], rand);
   int rc = cache_->StartSession();
-  if (rc == RAYT_OK) rc = cache_->StartTransaction();
+  if (rc == RAYT_OK) rc = cache_->StartTransaction((int)fb_.faults.size());
   if (rc == RAYT_OK) {
     cache_->MarkUsedBatch(fb_.hits, fb_.dup_hits);
     for (int b : fb_.faults) {
