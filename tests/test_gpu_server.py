@@ -106,6 +106,34 @@ def test_served_scheduler_thread_and_concurrent_submitters(trees):
             np.testing.assert_array_equal(img, _resident(trees, w, h, m), err_msg="client %d frame %d" % (v, f))
 
 
+def test_served_delivery_through_client_changes(trees):
+    """Host delivery while clients come and go: frames of two clients are
+    delivered (their copies overlapping the next ticks), one client is
+    removed right after its last frame and a client of another size takes
+    its slot; every delivered image equals the resident oracle frame."""
+    ld, cm, srv = _server(trees, max_blocks=0, deliver_to_host=True)  # resident: no request truncates
+    a = srv.add_client(96, 64)
+    b = srv.add_client(160, 90)
+    for f in range(3):
+        ma, mb = _matrix(_cam(25.0 * f, 0), 96, 64), _matrix(_cam(25.0 * f + 90, 1), 160, 90)
+        ra, rb = srv.submit(a, ma), srv.submit(b, mb)
+        srv.wait(ra)
+        np.testing.assert_array_equal(srv.host_image(a), _resident(trees, 96, 64, ma), err_msg="a %d" % f)
+        srv.wait(rb)
+        np.testing.assert_array_equal(srv.host_image(b), _resident(trees, 160, 90, mb), err_msg="b %d" % f)
+    srv.remove_client(b)
+    c = srv.add_client(128, 128)
+    for f in range(2):
+        ma, mc = _matrix(_cam(40.0 * f + 10, 0), 96, 64), _matrix(_cam(40.0 * f + 200, 2), 128, 128)
+        ra, rc = srv.submit(a, ma), srv.submit(c, mc)
+        srv.wait(rc)
+        np.testing.assert_array_equal(srv.host_image(c), _resident(trees, 128, 128, mc), err_msg="c %d" % f)
+        srv.wait(ra)
+        np.testing.assert_array_equal(srv.host_image(a), _resident(trees, 96, 64, ma), err_msg="a' %d" % f)
+    assert srv.stats()["completed"] == 10
+    srv.close()
+
+
 def test_served_admission_limits(trees):
     # framebuffer memory admits clients: 2 frames of 128x128 fit, a third does not
     ld, cm, srv = _server(trees, framebuffer_bytes=2 * 128 * 128 * 4)
