@@ -20,7 +20,7 @@ def _pinned(nbytes):
     return torch.empty(nbytes, dtype=torch.uint8).pin_memory()
 
 
-def _pair(path, max_blocks, w, h, lod, seed, max_passes=0):
+def _pair(path, max_blocks, w, h, lod, seed, max_passes=0, extras=False):
     out = []
     for _ in range(2):
         ld = R.StoredOctreeLoader(path)
@@ -32,6 +32,9 @@ def _pair(path, max_blocks, w, h, lod, seed, max_passes=0):
         rt.seed(seed)
         if max_passes:
             rt.set_max_passes(max_passes)
+        if extras:  # depth output, and plain launches (recorded passes) instead of pass graphs
+            rt.set_depth_output(True)
+            rt.record_passes(True)
         out.append((ld, cm, rt))
     return out
 
@@ -40,12 +43,14 @@ def _matrix(cam, w, h):
     return R.Camera(cam[0], cam[1], cam[2], cam[3:6], cam[6], w / h).view_proj_inv()
 
 
-@pytest.mark.parametrize("name,max_passes", [("stream8", 0), ("stream8_lod0", 0), ("c1_stream", 0), ("stream8", 2)])
-def test_host_image_equals_device_image(trees, name, max_passes):
+@pytest.mark.parametrize("name,max_passes,extras", [("stream8", 0, False), ("stream8_lod0", 0, False),
+                                                    ("c1_stream", 0, False), ("stream8", 2, False),
+                                                    ("stream8", 0, True)])
+def test_host_image_equals_device_image(trees, name, max_passes, extras):
     case = FRAME_CASES[name]
     w, h = case["size"]
     (_, _, plain), (_, _, deliv) = _pair(trees[case["tree"]], case["max_blocks"], w, h, case["lod"], case["seed"],
-                                         max_passes)
+                                         max_passes, extras)
     buf = _pinned(w * h * 4)
     deliv.set_host_image(buf.data_ptr(), buf.numel())
     multi, stopped = 0, 0
@@ -57,6 +62,11 @@ def test_host_image_equals_device_image(trees, name, max_passes):
         host = buf.numpy().reshape(h, w, 4).copy()
         assert np.array_equal(host, deliv.read_image())
         assert np.array_equal(host, plain.read_image())
+        if extras:
+            dd, dn = deliv.read_depth()
+            pd, pn = plain.read_depth()
+            assert np.array_equal(np.asarray(dd).view(np.uint32), np.asarray(pd).view(np.uint32))
+            assert np.array_equal(dn, pn)
         st = deliv.stats()
         multi += st["passes"] > 1
         stopped += st["passes"] == max_passes
